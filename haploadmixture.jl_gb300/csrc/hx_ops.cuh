@@ -1,0 +1,64 @@
+// hx_ops.cuh -- declarations of the non-pass kernels and launchers (hx_ops.cu)
+// and of the pass launchers (hx_pass_f64.cu / hx_pass_f32.cu).
+#pragma once
+#include "hx_pass.cuh"
+
+namespace hx {
+
+// Slots of the per-context device scalar block (double[HX_NSLOT]).
+enum Slot {
+    S_LL_NEW = 0, S_LL_PREV = 1, S_LL_BASIC = 2, S_LL_QN = 3, S_RELDIFF = 4, S_ACCEPT_QN = 5,
+    S_ITER = 6, S_TMP = 7, S_QP_FAIL = 8, S_NAN = 9, HX_NSLOT = 16
+};
+
+// pass launchers: precision-specific translation units
+cudaError_t launch_accum_q_f64(int K, bool hess, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_accum_p_f64(int K, bool hess, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_loglik_f64(int K, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_accum_q_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_accum_p_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
+
+// decode / checks / synthetic data
+cudaError_t launch_pack(const uint8_t* bed, int64_t bps, int64_t I, int64_t J, int64_t Ipad, int JW, uint32_t* G,
+                        cudaStream_t st);
+cudaError_t launch_census(const uint32_t* G, int64_t Ipad, int64_t I, int64_t J, int JW,
+                          unsigned long long* counts, cudaStream_t st);
+cudaError_t launch_double_missing(const uint8_t* bed, int64_t bps, int64_t I, int64_t nsnp,
+                                  unsigned long long* dm, cudaStream_t st);
+cudaError_t launch_synth(uint64_t seed, int64_t I, int64_t J, int K, const uint64_t* thrQ, const uint64_t* thrP,
+                         double miss, uint8_t* bed, cudaStream_t st);
+
+// reductions of pass partials
+cudaError_t launch_reduce_sym(const double* part, int S, int K, bool hess, int64_t rows, int64_t ld,
+                              double* XtX, double* Xtz, cudaStream_t st);
+cudaError_t launch_reduce_sum(const double* part, int64_t n, double* out, cudaStream_t st);
+
+// EM normalisation + projection (algorithms_inner.jl:66-76)
+cudaError_t launch_em_q(const double* q, const double* Xtz, const unsigned long long* dm, int64_t J, int K,
+                        int64_t I, double eps, double* q_next, cudaStream_t st);
+cudaError_t launch_em_p(const double* p, const double* Xtz, int K, int64_t J, double eps, double* p_next,
+                        cudaStream_t st);
+// q_next = project(q + d) per column / quartet; d may be null (plain projection)
+cudaError_t launch_step_q(const double* q, const double* d, int K, int64_t ncol, double eps, double* out,
+                          cudaStream_t st);
+cudaError_t launch_step_p(const double* p, const double* d, int K, int64_t J, double eps, double* out,
+                          cudaStream_t st);
+// batched QP (init_kernel_attrs: once per device, before the first launch)
+cudaError_t init_kernel_attrs();
+cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff,
+                        double* slots, cudaStream_t st);
+cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
+                        double* pdiff, double* slots, cudaStream_t st);
+// ZAL quasi-Newton
+int qn_dots_blocks(int64_t n);
+cudaError_t launch_qn(int64_t n, const double* x, const double* xn, const double* xn2, double* U, double* V,
+                      int Qs, double* part, double* coef, double* xt, double* slots, cudaStream_t st);
+// outer-iteration bookkeeping
+cudaError_t launch_iter_begin(double* slots, cudaStream_t st);
+cudaError_t launch_accept(int64_t n, double* x, const double* xt, const double* xn2, double* slots,
+                          cudaStream_t st);
+cudaError_t launch_copy_slot(double* slots, int dst, int src, cudaStream_t st);
+cudaError_t launch_nan_check(const double* a, int64_t n, double* slots, cudaStream_t st);
+
+}  // namespace hx

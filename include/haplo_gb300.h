@@ -1,0 +1,177 @@
+/* haplo_gb300.h -- C ABI of the GB300 (sm_103a) HaploADMIXTURE fitting path.
+ *
+ * One context (hx_ctx) owns, for its whole lifetime, all device memory of one
+ * fit on one GPU: the decoded genotype classes, the Q/P iterates of
+ * AdmixData2 (x, x_next, x_next2, x_tmp; K x (I+4J) FP64, Julia column-major),
+ * the gradient/Hessian buffers, the ZAL secant matrices U/V and the scratch of
+ * the reductions.  Host buffers are owned by the caller; the library copies
+ * them in or out during the call and never keeps a host pointer.
+ *
+ * Layouts follow the reference's Julia arrays (column-major, 0-based here):
+ *   bed   : PLINK 1 .bed data bytes after the 3-byte magic, SNP-major,
+ *           bytes_per_snp = ceil(N_file/4) bytes per SNP (SnpArray.data)
+ *   q     : K x I            q[k + K*i]
+ *   p     : K x 4J           p[k + K*m], m = 4j + h, h in {00,01,10,11}
+ *   XtX_q : K x K x I        XtX[k2 + K*k + K*K*i]      Xtz_q : K x I
+ *   XtX_p : K x K x 4J       XtX[k2 + K*k + K*K*m]      Xtz_p : K x 4J
+ *
+ * Every entry point returns an int status (HX_OK = 0).  hx_last_error()
+ * returns the context's last message.  No C++ exception crosses the ABI.
+ * A context is used by one host thread at a time; distinct contexts are
+ * independent.  There is no CPU fallback: without a usable CUDA device
+ * hx_create returns HX_ECUDA.
+ */
+#ifndef HAPLO_GB300_H
+#define HAPLO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HX_OK 0
+#define HX_EINVAL 1        /* bad argument or size */
+#define HX_ECUDA 2         /* CUDA runtime error, or no device */
+#define HX_ENAN 3          /* NaN in a gradient/Hessian (src/algorithms_inner.jl:132-133) */
+#define HX_ETIMEOUT 4      /* an iteration cap was hit */
+#define HX_ENOMEM 5        /* device allocation failed */
+#define HX_ESTATE 6        /* call out of order (e.g. no Q/P set yet) */
+#define HX_EUNSUPPORTED 7  /* K outside 1..HX_KMAX, or secant count outside 1..HX_QMAX */
+
+#define HX_KMAX 12
+#define HX_QMAX 6
+
+#define HX_PREC_FP64 0     /* plain method: every pass in FP64 */
+#define HX_PREC_MIXED 1    /* FP32 per-pair arithmetic, FP64 totals, FP64 QP/QN */
+
+typedef struct hx_ctx hx_ctx;
+
+typedef struct hx_opts {
+    int32_t precision;     /* HX_PREC_FP64 (default) or HX_PREC_MIXED */
+    int32_t device;        /* CUDA device ordinal (default 0) */
+    int32_t Qsec;          /* secant pairs of the QN step, AdmixData2.Q (default 3; driver.jl:50) */
+    int32_t verbose;       /* 1: one JSON line per outer iteration on stderr */
+    double rho;            /* P-step penalty (default 1e7; algorithms_inner.jl:225) */
+    double pseudocount;    /* projection floor (default 1e-5; utils.jl:20) */
+} hx_opts;
+
+typedef struct hx_iter_info {
+    int32_t iter;          /* outer iteration number (1-based) */
+    int32_t accepted_qn;   /* 1 if the ZAL point was kept (algorithms_outer.jl:154-160) */
+    double ll_prev, ll_basic, ll_qn, ll_new, reldiff;
+    double seconds;        /* device time of the iteration */
+} hx_iter_info;
+
+typedef struct hx_fit_info {
+    int32_t iters;         /* outer iterations run */
+    int32_t converged;     /* reldiff < rtol reached */
+    int32_t em_iters;      /* EM iterations run before the QN loop */
+    int32_t pad_;
+    double ll;             /* final log-likelihood (d.ll_new) */
+    double seconds;        /* wall time of the call */
+} hx_fit_info;
+
+/* Defaults: precision FP64, device 0, Qsec 3, rho 1e7, pseudocount 1e-5. */
+int hx_opts_default(hx_opts* opts);
+const char* hx_status_string(int status);
+const char* hx_last_error(const hx_ctx* ctx);
+
+/* Replaces _cu_admixture_base / CuAdmixData (src/cuda/structs.jl:16-44,
+ * src/driver.jl:203-205): uploads the first I individuals x first 2J SNPs of
+ * the BED matrix (host memory), decodes them once into class words, counts
+ * double-missing blocks over all n_snp SNPs (src/utils.jl:1-18).  Q/P are
+ * unset until hx_set_qp. */
+int hx_create(const uint8_t* bed, int64_t bytes_per_snp, int64_t n_snp, int64_t I, int64_t J, int32_t K,
+              const hx_opts* opts, hx_ctx** out);
+/* Same, with the BED matrix already in device memory of opts->device. */
+int hx_create_device(const uint8_t* d_bed, int64_t bytes_per_snp, int64_t n_snp, int64_t I, int64_t J,
+                     int32_t K, const hx_opts* opts, hx_ctx** out);
+int hx_destroy(hx_ctx* ctx);
+int hx_dims(const hx_ctx* ctx, int64_t* I, int64_t* J, int32_t* K);
+
+/* State (AdmixData2.q / .p, src/structs.jl:36-46).  which: 0 x, 1 x_next,
+ * 2 x_next2, 3 x_tmp.  q/p may be NULL to skip one of them. */
+int hx_set_qp(hx_ctx* ctx, const double* q, const double* p);
+int hx_set_qp_device(hx_ctx* ctx, const double* d_q, const double* d_p);
+int hx_get_qp(hx_ctx* ctx, int32_t which, double* q, double* p);
+/* d.ll_new (NaN until computed) */
+int hx_get_ll(hx_ctx* ctx, double* ll_new);
+
+/* Genotype checks: 16-class census, index g1*4+g2 with missing = 3 (bit-exact
+ * integer counts over the I x J pairs), and double-missing counts per individual. */
+int hx_census(hx_ctx* ctx, uint64_t counts[16]);
+int hx_double_missing(hx_ctx* ctx, int64_t* dm);
+
+/* ---- the reference's GPU runners (src/cuda/runners.jl), on host arrays ---- */
+/* loglikelihood(d_cu, g_cu, q, p) (runners.jl:13-16).  q/p NULL -> device x. */
+int hx_loglikelihood(hx_ctx* ctx, const double* q, const double* p, double* ll);
+/* em!(d_cu, g_cu) raw numerators (runners.jl:45-49; kernels.jl:42-73). */
+int hx_em_accum(hx_ctx* ctx, const double* q, const double* p, double* q_next, double* p_next);
+/* update_q_cuda!(d_cu, g_cu) (runners.jl:71-74; kernels.jl:104-138). */
+int hx_update_q_accum(hx_ctx* ctx, const double* q, const double* p, double* XtX, double* Xtz);
+/* update_p_cuda!(d_cu, g_cu) (runners.jl:89-92; kernels.jl:140-175). */
+int hx_update_p_accum(hx_ctx* ctx, const double* q, const double* p, double* XtX, double* Xtz);
+
+/* ---- batched QP / projection (CPU-only in the reference) on host arrays ---- */
+/* Per individual: argmin 0.5 d'Hd - g'd, sum d = 0, 0 <= q+d <= 1 with
+ * H = XtX[:,:,i], g = Xtz[:,i] (algorithms_inner.jl:134-168). n individuals. */
+int hx_qp_q(hx_ctx* ctx, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff);
+/* Per block: 4K variables, H = blockdiag(XtX[:,:,4j+h]) + rho on the
+ * (h,h2,k) pattern, 0 <= p+d <= 1 (algorithms_inner.jl:264-305). n blocks. */
+int hx_qp_p(hx_ctx* ctx, int64_t n, const double* XtX, const double* Xtz, const double* p, double* pdiff);
+/* OpenADMIXTURE.project_q! per column / project_p! per (k, block) quartet. */
+int hx_project_q(hx_ctx* ctx, int64_t ncol, double* q);
+int hx_project_p(hx_ctx* ctx, int64_t nblocks, double* p);
+/* ZAL quasi-Newton point (update_UV! + update_QN!, algorithms_outer.jl:129-133)
+ * on host vectors of length n = K(I+4J): U/V are n x Qsec and are updated. */
+int hx_zal(hx_ctx* ctx, const double* x, const double* x_next, const double* x_next2, double* U, double* V,
+           int32_t iter, double* x_tmp);
+
+/* ---- device-resident algorithm steps (algorithms_inner.jl / _outer.jl) ---- */
+/* em! (algorithms_inner.jl:29-84): x -> x_next (normalised, projected). */
+int hx_em_step(hx_ctx* ctx);
+/* init_em! (algorithms_outer.jl:1-22): iters EM steps; sets d.ll_new. */
+int hx_init_em(hx_ctx* ctx, int32_t iters);
+/* update_q!(d, g, update2) / update_p!(d, g, update2) (algorithms_inner.jl:97-355). */
+int hx_update_q(hx_ctx* ctx, int32_t update2);
+int hx_update_p(hx_ctx* ctx, int32_t update2);
+/* One outer iteration of admixture_qn! (algorithms_outer.jl:65-171, :ZAL). */
+int hx_qn_iteration(hx_ctx* ctx, hx_iter_info* info);
+/* admixture_qn!(d, g, n_iter, rtol; iter_count_offset) (algorithms_outer.jl:38-172). */
+int hx_admixture_qn(hx_ctx* ctx, int32_t n_iter, double rtol, int32_t iter_offset, hx_fit_info* info);
+/* _admixture_base's fit sequence (driver.jl:181-197): init_em! (em_iters) then
+ * admixture_qn!.  Starts from the current x. */
+int hx_fit(hx_ctx* ctx, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_info* info);
+
+/* ---- launch accounting (no counterpart in the reference, which prints
+ * @time per phase, src/algorithms_inner.jl:114,135,241,259) ---- */
+#define HX_KIND_ACCUM_Q 0  /* Q-side gradient/Hessian pass */
+#define HX_KIND_ACCUM_P 1  /* P-side gradient/Hessian pass */
+#define HX_KIND_LOGLIK 2   /* log-likelihood pass */
+#define HX_KIND_QP_Q 3     /* batched per-individual QP */
+#define HX_KIND_QP_P 4     /* batched per-block QP */
+#define HX_KIND_QN 5       /* ZAL secant update, solve and step */
+#define HX_KIND_OTHER 6    /* reductions, projections, bookkeeping */
+#define HX_NKIND 7
+/* on != 0: record CUDA events around every launch on the context's stream. */
+int hx_set_profiling(hx_ctx* ctx, int32_t on);
+/* Launches issued (always counted) and device ms (while profiling) of a kind. */
+int hx_kernel_stats(hx_ctx* ctx, int32_t kind, int64_t* launches, double* ms);
+int hx_reset_stats(hx_ctx* ctx);
+
+/* ---- synthetic cohorts ---- */
+/* Writes the SNP-major BED matrix (ceil(I/4) bytes per SNP, 2J SNPs) of a
+ * synthetic admixed cohort into device memory d_bed: per (i, j) two haplotype
+ * copies with ancestry z ~ Cat(Q_i) and haplotype h ~ Cat(P_{z,j}); missing at
+ * rate miss per (i, SNP).  thrQ (K x I) and thrP (K x 4J) are the cumulative
+ * probabilities as integer thresholds ceil(cum * 2^53) (last entry may be any
+ * value >= 2^53).  Counter-based SplitMix64 draws: the bytes equal those of the
+ * CPU generator bit for bit. */
+int hx_synth_bed_device(uint64_t seed, int64_t I, int64_t J, int32_t K, const uint64_t* thrQ,
+                        const uint64_t* thrP, double miss, uint8_t* d_bed, int32_t device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,192 @@
+"""GPU parity: every device pass / solver / step through the C ABI against the
+CPU oracle on the same seeded inputs.
+
+Tolerances: integer work (decode, census, double-missing counts, synthetic
+genotypes) is bit-exact.  The plain FP64 method agrees with the FP64 oracle to
+1e-10 relative (log-likelihood, gradient, Hessian; scale = largest entry).
+QP/projection/ZAL results agree to 1e-9 relative.  The mixed method (FP32
+per-pair arithmetic, FP64 totals) is held to 1e-5 relative on the gradient,
+1e-3 on the Hessian and 1e-8 on the log-likelihood.
+"""
+import numpy as np
+import pytest
+
+from conftest import small_cohort
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def make(hx, c, precision="fp64", **kw):
+    return hx.GB300Admix(c["bed"], c["I"], c["J"], c["K"], bytes_per_snp=c["bed"].shape[1],
+                         n_snp=c["bed"].shape[0], precision=precision, **kw)
+
+
+def start(c, seed=3):
+    from haplo_gb300.admix import random_init
+    return random_init(c["I"], c["J"], c["K"], np.random.default_rng(seed))
+
+
+@pytest.fixture(scope="module")
+def coh():
+    return small_cohort(333, 203, 3, seed=17, extra_snps=6)
+
+
+def test_census_and_double_missing_bit_exact(hx, O, coh):
+    d = make(hx, coh)
+    b = O.Bed(coh["bed"], coh["I"], coh["J"], n_snp=coh["bed"].shape[0])
+    np.testing.assert_array_equal(d.census(), O.census(b))
+    np.testing.assert_array_equal(d.double_missing(), O.double_missing(b))
+    assert int(d.census().sum()) == coh["I"] * coh["J"]
+
+
+@pytest.mark.parametrize("I,J,K", [(1, 1, 1), (5, 9, 2), (130, 17, 4), (333, 203, 7)])
+def test_device_generator_matches_cpu_bytes(hx, O, I, J, K):
+    import torch
+    from haplo_gb300 import synth
+    Q, P = synth.draw_params(I, J, K, 0.4, "dirichlet", seed=I + J + K)
+    cq, cp = synth.cumulative(Q, P)
+    want = O.synth(99, I, J, cq, cp, 0.03)
+    buf = torch.zeros(want.size, dtype=torch.uint8, device="cuda")
+    synth.synth_device(99, Q, P, 0.03, buf.data_ptr())
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(buf.cpu().numpy().reshape(want.shape), want)
+
+
+@pytest.mark.parametrize("K", list(range(1, 13)))
+def test_loglik_and_accumulations_fp64_all_K(hx, O, K):
+    c = small_cohort(141, 37, K, seed=100 + K, miss=0.05)
+    b = O.Bed(c["bed"], c["I"], c["J"])
+    q, p = start(c, seed=K)
+    d = make(hx, c)
+    assert d.loglikelihood(q, p) == pytest.approx(O.loglik(b, K, q, p), rel=1e-12)
+    XtX, Xtz = d.update_q_accum(q, p)
+    oX, oz = O.accum_q(b, K, q, p)
+    assert rel_err(Xtz, oz) < 1e-12 and rel_err(XtX, oX) < 1e-12
+    XtX, Xtz = d.update_p_accum(q, p)
+    oX, oz = O.accum_p(b, K, q, p)
+    assert rel_err(Xtz, oz) < 1e-12 and rel_err(XtX, oX) < 1e-12
+    qn, pn = d.em_accum(q, p)
+    oq, op = O.em_accum(b, K, q, p)
+    assert rel_err(qn, oq) < 1e-12 and rel_err(pn, op) < 1e-12
+
+
+def test_loglik_formulas_and_injected_state(hx, O, coh):
+    b = O.Bed(coh["bed"], coh["I"], coh["J"])
+    q, p = start(coh)
+    d = make(hx, coh)
+    d.set_qp(q, p)
+    want = O.loglik(b, coh["K"], q, p, formula=1)
+    assert d.loglikelihood() == pytest.approx(want, rel=1e-12)
+    assert d.loglikelihood(q, p) == pytest.approx(O.loglik(b, coh["K"], q, p, formula=2), rel=1e-12)
+
+
+def test_qp_and_projection_match_oracle(hx, O, coh):
+    b = O.Bed(coh["bed"], coh["I"], coh["J"])
+    K = coh["K"]
+    q, p = start(coh)
+    d = make(hx, coh)
+    XtX, Xtz = O.accum_q(b, K, q, p)
+    dq = d.qp_q(XtX, Xtz, q)
+    oq, f = O.qp_q(XtX, Xtz, q)
+    assert f == 0 and np.abs(dq - oq).max() < 1e-9
+    XtXp, Xtzp = O.accum_p(b, K, q, p)
+    dp = d.qp_p(XtXp, Xtzp, p)
+    op, f = O.qp_p(XtXp, Xtzp, p)
+    assert f == 0 and np.abs(dp - op).max() < 1e-9
+    rng = np.random.default_rng(0)
+    V = rng.normal(size=(K, 500)) * 0.5 + 1.0 / K
+    np.testing.assert_allclose(d.project_q(V), O.project_q(V), atol=1e-15)
+    W = rng.normal(size=(K, 400)) * 0.5 + 0.25
+    np.testing.assert_allclose(d.project_p(W), O.project_p(W), atol=1e-15)
+
+
+def test_zal_matches_oracle(hx, O, coh):
+    d = make(hx, coh)
+    n = coh["K"] * (coh["I"] + 4 * coh["J"])
+    rng = np.random.default_rng(4)
+    U = np.zeros((n, 3))
+    V = np.zeros((n, 3))
+    Uo, Vo = U.copy(), V.copy()
+    for it in range(1, 6):
+        x, xn, xn2 = rng.normal(size=(3, n))
+        xt, U, V = d.zal(x, xn, xn2, U, V, it)
+        xo, Uo, Vo = O.zal(x, xn, xn2, Uo, Vo, it)
+        np.testing.assert_allclose(U, Uo, rtol=0, atol=0)
+        assert rel_err(xt, xo) < 1e-9
+
+
+def test_update_steps_match_oracle(hx, O, coh):
+    b = O.Bed(coh["bed"], coh["I"], coh["J"])
+    K = coh["K"]
+    q, p = start(coh)
+    d = make(hx, coh)
+    d.set_qp(q, p)
+    d.update_q(False)
+    qn_d = d.get_qp("x_next")[0]
+    qn_o, _ = O.update_q(b, K, q, p)
+    assert np.abs(qn_d - qn_o).max() < 1e-9
+    d.update_p(False)
+    pn_d = d.get_qp("x_next")[1]
+    pn_o, _ = O.update_p(b, K, qn_o, p)
+    assert np.abs(pn_d - pn_o).max() < 1e-9
+    d.set_qp(q, p)
+    d.em_step()
+    qe, pe = d.get_qp("x_next")
+    oqe, ope = O.em_step(b, K, q, p)
+    assert np.abs(qe - oqe).max() < 1e-12 and np.abs(pe - ope).max() < 1e-12
+
+
+def test_fit_matches_oracle_fp64(hx, O):
+    c = small_cohort(400, 300, 3, seed=21, alpha=0.5, miss=0.01)
+    b = O.Bed(c["bed"], c["I"], c["J"])
+    q0, p0 = start(c, seed=1)
+    qo, po, llo, ito, tro = O.fit(b, 3, q0, p0, n_iter=300, rtol=1e-7)
+    d = make(hx, c)
+    d.set_qp(q0, p0)
+    info = d.fit(n_iter=300, rtol=1e-7, em_iters=5)
+    qd, pd = d.get_qp()
+    assert info["ll"] == pytest.approx(llo, rel=1e-9)
+    assert abs(info["iters"] - ito) <= 1
+    assert np.abs(qd - qo).max() < 1e-5
+    assert info["ll"] == pytest.approx(d.loglikelihood(qd, pd), rel=1e-12)
+
+
+def test_mixed_precision_passes(hx, O, coh):
+    b = O.Bed(coh["bed"], coh["I"], coh["J"])
+    K = coh["K"]
+    q, p = start(coh)
+    d = make(hx, coh, precision="mixed")
+    assert d.loglikelihood(q, p) == pytest.approx(O.loglik(b, K, q, p), rel=1e-8)
+    XtX, Xtz = d.update_q_accum(q, p)
+    oX, oz = O.accum_q(b, K, q, p)
+    assert rel_err(Xtz, oz) < 1e-5 and rel_err(XtX, oX) < 1e-3
+    XtX, Xtz = d.update_p_accum(q, p)
+    oX, oz = O.accum_p(b, K, q, p)
+    assert rel_err(Xtz, oz) < 1e-5 and rel_err(XtX, oX) < 1e-3
+
+
+def test_mixed_fit_reaches_fp64_optimum(hx, O):
+    c = small_cohort(400, 300, 3, seed=21, alpha=0.5, miss=0.01)
+    q0, p0 = start(c, seed=1)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        d = make(hx, c, precision=prec)
+        d.set_qp(q0, p0)
+        info = d.fit(n_iter=500, rtol=1e-9, em_iters=5)
+        out[prec] = (info, d.get_qp()[0])
+    assert out["mixed"][0]["ll"] == pytest.approx(out["fp64"][0]["ll"], rel=1e-8)
+    assert np.abs(out["mixed"][1] - out["fp64"][1]).max() < 1e-4
+
+
+def test_errors_are_status_codes(hx, coh):
+    from haplo_gb300 import HxError
+    with pytest.raises(HxError):
+        hx.GB300Admix(coh["bed"], coh["I"], coh["J"], 13)          # K above HX_KMAX
+    d = make(hx, coh)
+    with pytest.raises(HxError):
+        d.update_q()                                               # Q/P not set yet
