@@ -497,7 +497,8 @@ k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn
           double* __restrict__ U, double* __restrict__ V, const double* __restrict__ slots, double* __restrict__ part) {
     constexpr int NV = QS * QS * 2 + QS;   // UtU (full), UtV, Utd
     __shared__ double red[QN_THREADS / 32][NV];
-    const int col = ((int)slots[S_ITER] - 1) % QS;
+    const int it = (int)slots[S_ITER];
+    const int col = (it > 0 ? it - 1 : 0) % QS;
     double acc[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) acc[v] = 0.0;

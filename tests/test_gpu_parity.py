@@ -171,16 +171,19 @@ def test_mixed_precision_passes(hx, O, coh):
 
 
 def test_mixed_fit_reaches_fp64_optimum(hx, O):
+    # both fits run to (near) full convergence, so that the comparison is
+    # between optima and not between two early-stopped points of a flat
+    # likelihood (I=400, J=300 pins Q only loosely at rtol 1e-9)
     c = small_cohort(400, 300, 3, seed=21, alpha=0.5, miss=0.01)
     q0, p0 = start(c, seed=1)
     out = {}
     for prec in ("fp64", "mixed"):
         d = make(hx, c, precision=prec)
         d.set_qp(q0, p0)
-        info = d.fit(n_iter=500, rtol=1e-9, em_iters=5)
+        info = d.fit(n_iter=3000, rtol=1e-14, em_iters=5)
         out[prec] = (info, d.get_qp()[0])
-    assert out["mixed"][0]["ll"] == pytest.approx(out["fp64"][0]["ll"], rel=1e-8)
-    assert np.abs(out["mixed"][1] - out["fp64"][1]).max() < 1e-4
+    assert out["mixed"][0]["ll"] == pytest.approx(out["fp64"][0]["ll"], rel=1e-9)
+    assert np.abs(out["mixed"][1] - out["fp64"][1]).max() < 2e-5
 
 
 def test_errors_are_status_codes(hx, coh):
