@@ -36,6 +36,8 @@ struct hx_ctx {
     double* slots = nullptr;
     double* h_slots = nullptr;   // pinned
     int S_q = 1, wpc_q = 1, S_p = 1, ipc_p = 1;
+    bool tc = false;                         // Hessian passes on the tensor cores
+    int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
     bool have_qp = false;
     std::string err;
     // launch accounting: per kind, kernel launches issued and (when profiling
@@ -128,6 +130,20 @@ void plan(hx_ctx* c) {
     ipc = (ipc + PSTAGE_IND - 1) / PSTAGE_IND * PSTAGE_IND;
     c->ipc_p = (int)ipc;
     c->S_p = (int)((c->I + ipc - 1) / ipc);
+    // tensor-core passes: one 256-thread CTA per SM; aim for >= 8 waves of 152
+    const int64_t target_tc = 8 * 152;
+    int64_t St = std::max<int64_t>(1, (target_tc + tilesQ - 1) / tilesQ);
+    St = std::min<int64_t>(St, (c->JW + 1) / 2);
+    int64_t wpc = (c->JW + St - 1) / St;
+    wpc = (wpc + 1) / 2 * 2;                 // whole stages of 2 words (16 blocks)
+    c->wpc_qt = (int)wpc;
+    c->S_qt = (int)((c->JW + wpc - 1) / wpc);
+    int64_t Spt = std::max<int64_t>(1, (target_tc + tilesP - 1) / tilesP);
+    Spt = std::min<int64_t>(Spt, (c->I + 63) / 64);
+    int64_t ipt = (c->I + Spt - 1) / Spt;
+    ipt = (ipt + 63) / 64 * 64;              // whole stages of 64 individuals
+    c->ipc_pt = (int)ipt;
+    c->S_pt = (int)((c->I + ipt - 1) / ipt);
 }
 
 PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
@@ -135,11 +151,18 @@ PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
     a.G = c->G; a.Ipad = c->Ipad; a.I = c->I; a.J = c->J; a.JW = c->JW;
     a.q = q; a.p = p; a.S = 1; a.per_chunk = 1;
     a.part = nullptr; a.XtX = nullptr; a.Xtz = nullptr;
+    a.slots = c->slots;
     return a;
 }
 
 int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, double* Xtz) {
     PassArgs a = pass_args(c, q, p);
+    if (hess && c->tc) {
+        a.S = c->S_qt; a.per_chunk = c->wpc_qt; a.part = c->part_q;
+        HX_LAUNCH(HX_KIND_ACCUM_Q, 1, launch_accum_q_tc(c->K, a, c->st));
+        HX_LAUNCH(HX_KIND_OTHER, 1, launch_reduce_sym(c->part_q, c->S_qt, c->K, true, c->I, c->Ipad, XtX, Xtz, c->st));
+        return HX_OK;
+    }
     a.S = c->S_q; a.per_chunk = c->wpc_q; a.part = c->part_q;
     HX_LAUNCH(HX_KIND_ACCUM_Q, 1,
               c->prec == HX_PREC_FP64 ? launch_accum_q_f64(c->K, hess, a, c->st)
@@ -150,6 +173,14 @@ int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
 
 int pass_p(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, double* Xtz) {
     PassArgs a = pass_args(c, q, p);
+    if (hess && c->tc) {
+        a.S = c->S_pt; a.per_chunk = c->ipc_pt; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;
+        HX_LAUNCH(HX_KIND_ACCUM_P, 1, launch_accum_p_tc(c->K, a, c->st));
+        if (c->S_pt > 1)
+            HX_LAUNCH(HX_KIND_OTHER, 1,
+                      launch_reduce_sym(c->part_p, c->S_pt, c->K, true, 4 * c->J, 4 * c->J, XtX, Xtz, c->st));
+        return HX_OK;
+    }
     a.S = c->S_p; a.per_chunk = c->ipc_p; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;
     HX_LAUNCH(HX_KIND_ACCUM_P, 1,
               c->prec == HX_PREC_FP64 ? launch_accum_p_f64(c->K, hess, a, c->st)
@@ -261,6 +292,7 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     *out = c;
     c->device = o.device; c->prec = o.precision; c->Qs = o.Qsec; c->verbose = o.verbose;
     c->rho = o.rho; c->eps = o.pseudocount;
+    c->tc = (o.precision == HX_PREC_MIXED) && (o.path == HX_PATH_AUTO);
     c->I = I; c->J = J; c->K = K; c->nsnp = nsnp; c->bps = bps;
     c->Ipad = (I + HX_IPAD - 1) / HX_IPAD * HX_IPAD;
     c->JW = (int)((J + 7) / 8);
@@ -273,6 +305,7 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_CK(cudaEventCreate(&c->ev0));
     HX_CK(cudaEventCreate(&c->ev1));
     HX_CK(init_kernel_attrs());
+    HX_CK(init_tc_attrs());
     plan(c);
     const int NVmax = K + K * (K + 1) / 2;
     HX_ST(dalloc(c, &c->G, (size_t)c->JW * c->Ipad));
@@ -284,8 +317,9 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_ST(dalloc(c, &c->Xtzq, (size_t)K * I));
     HX_ST(dalloc(c, &c->XtXp, (size_t)K * K * 4 * J));
     HX_ST(dalloc(c, &c->Xtzp, (size_t)K * 4 * J));
-    HX_ST(dalloc(c, &c->part_q, (size_t)c->S_q * NVmax * c->Ipad));
-    if (c->S_p > 1) HX_ST(dalloc(c, &c->part_p, (size_t)c->S_p * NVmax * 4 * J));
+    HX_ST(dalloc(c, &c->part_q, (size_t)std::max(c->S_q, c->tc ? c->S_qt : 1) * NVmax * c->Ipad));
+    const int Sp_max = std::max(c->S_p, c->tc ? c->S_pt : 1);
+    if (Sp_max > 1) HX_ST(dalloc(c, &c->part_p, (size_t)Sp_max * NVmax * 4 * J));
     HX_ST(dalloc(c, &c->part_ll, (size_t)(c->Ipad / ACC_THREADS) * c->S_q));
     HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (2 * HX_QMAX * HX_QMAX + HX_QMAX)));
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
@@ -356,6 +390,8 @@ int hx_opts_default(hx_opts* o) {
     o->verbose = 0;
     o->rho = 1e7;
     o->pseudocount = 1e-5;
+    o->path = HX_PATH_AUTO;
+    o->reserved = 0;
     return HX_OK;
 }
 
@@ -693,6 +729,7 @@ int hx_qn_iteration(hx_ctx* c, hx_iter_info* info) {
                 "\"qn\": %d, \"ms\": %.3f}\n",
                 (int)s[S_ITER], s[S_LL_NEW], s[S_RELDIFF], s[S_LL_BASIC], s[S_LL_QN], (int)s[S_ACCEPT_QN], ms);
     if (s[S_NAN] != 0.0) return fail(c, HX_ENAN, "NaN in XtX_q/Xtz_q");
+    if (s[S_TC_TIMEOUT] != 0.0) return fail(c, HX_ETIMEOUT, "tensor-core pass wait timed out");
     return HX_OK;
 }
 

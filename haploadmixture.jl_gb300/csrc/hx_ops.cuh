@@ -8,7 +8,7 @@ namespace hx {
 // Slots of the per-context device scalar block (double[HX_NSLOT]).
 enum Slot {
     S_LL_NEW = 0, S_LL_PREV = 1, S_LL_BASIC = 2, S_LL_QN = 3, S_RELDIFF = 4, S_ACCEPT_QN = 5,
-    S_ITER = 6, S_TMP = 7, S_QP_FAIL = 8, S_NAN = 9, HX_NSLOT = 16
+    S_ITER = 6, S_TMP = 7, S_QP_FAIL = 8, S_NAN = 9, S_TC_TIMEOUT = 10, HX_NSLOT = 16
 };
 
 // pass launchers: precision-specific translation units
@@ -18,6 +18,11 @@ cudaError_t launch_loglik_f64(int K, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_q_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_p_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
+
+// tensor-core (tcgen05) Hessian+gradient passes of the mixed method (hx_tc.cu)
+cudaError_t init_tc_attrs();
+cudaError_t launch_accum_q_tc(int K, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_accum_p_tc(int K, const PassArgs& a, cudaStream_t st);
 
 // decode / checks / synthetic data
 cudaError_t launch_pack(const uint8_t* bed, int64_t bps, int64_t I, int64_t J, int64_t Ipad, int JW, uint32_t* G,

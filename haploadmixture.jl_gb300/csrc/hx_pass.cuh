@@ -45,6 +45,7 @@ struct PassArgs {
     double* part;           // [S][NV][rows] partials, or null when S == 1 (P side)
     double* XtX;            // direct outputs when S == 1 (P side)
     double* Xtz;
+    double* slots;          // per-context scalar block (tensor-core kernels record timeouts there)
 };
 
 template <int K> __device__ __forceinline__ constexpr int tri(int k, int k2) {

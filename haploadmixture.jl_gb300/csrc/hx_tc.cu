@@ -1,0 +1,535 @@
+// hx_tc.cu -- tensor-core (tcgen05) gradient/Hessian passes of the mixed method.
+//
+// Both accumulations are GEMMs whose A operand is generated on the fly from the
+// genotype classes:
+//   Q side (src/loops.jl:328-365):  H_i = sum_m W[i,m] PP[m,:],  g_i = sum_m U[i,m] P[m,:]
+//   P side (src/loops.jl:367-403):  H_m = sum_i W[i,m] QQ[i,:],  g_m = sum_i U[i,m] Q[i,:]
+// with m = 4j+h, U = c_h/qp_h, W = c_h/qp_h^2, PP[m,(k,k2)] = p[k,m] p[k2,m]
+// (upper triangle) and QQ[i,(k,k2)] = q[k,i] q[k2,i].  The CUDA cores evaluate
+// each (individual, block) pair once (qp, class, U, W) and write bf16 hi/lo
+// splits of U and W into shared memory; one thread issues
+// tcgen05.mma kind::f16 (bf16 x bf16 -> fp32 in TMEM) for hi*hi + hi*lo + lo*hi.
+// The Hessian operands use BF16 (8-bit exponent) because W spans ~1 .. 2e10,
+// beyond FP16's range: hi+lo carries 16 significant bits.  The gradient
+// operands use IEEE FP16 hi/lo (22 bits) under exact power-of-two scaling,
+// since the gradient fixes the optimum and the Hessian only the step.  TMEM accumulates FP32 over windows of TC_FLUSH
+// stages; each window is folded into registers (FP32, Kahan-compensated), and
+// chunk partials are summed in FP64 by the same reduction as the CUDA-core pass.
+//
+// Pipeline per stage: [wait MMA of stage s-2 done] -> stage inputs -> generate
+// A and B tiles (double-buffered) -> barrier -> one thread issues the MMAs and
+// commits to an mbarrier -> the previous TMEM window is flushed while the
+// tensor core works.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
+// slots[S_TC_TIMEOUT] and the CTA drains and exits.
+#include "hx_ops.cuh"
+#include "hx_tc.cuh"
+
+namespace hx {
+namespace {
+using namespace tc;
+
+constexpr int TC_THREADS = 256;
+constexpr int TC_FLUSH = 4;
+constexpr long long TC_BUDGET = 4000000000LL;
+constexpr int SBO_STD = 1024;     // 8 core matrices (64 reduction elements) per row group
+constexpr int LBO_STD = 128;
+constexpr int LBO_PAD = 144;      // P-side A: padded so the generator stores are bank-conflict free
+constexpr int SBO_PAD = 8 * LBO_PAD;
+constexpr int A_TILE_STD = 16 * SBO_STD;   // 128 rows x 64 bf16
+constexpr int A_TILE_PAD = 16 * SBO_PAD;
+// Gradient operands use IEEE FP16 hi/lo (22 significant bits) under exact
+// power-of-two scaling that keeps them in FP16's normal range:
+// U * 2^-2 <= 5e4 (U = c/qp <= 2/1e-5), P or Q * 2^12 in [0.04, 4096].
+constexpr float U_SCALE = 0.25f;
+constexpr float GB_SCALE = 4096.0f;
+constexpr double G_UNSCALE = 1.0 / 1024.0;
+
+template <int K> struct TcDims {
+    static constexpr int NH = K * (K + 1) / 2;
+    static constexpr int NHP = (NH + 15) / 16 * 16;
+    static constexpr int NG = 16;
+    static constexpr int NT = NHP + NG;
+    static constexpr int TCOLS = (2 * NT <= 32) ? 32 : (2 * NT <= 64) ? 64 : (2 * NT <= 128) ? 128 : 256;
+    static constexpr int HALF = NT / 2;
+    static constexpr int B_TILE = NT * 128;    // NT rows x 64 bf16
+};
+
+struct Sync {
+    uint64_t mma_done[2];
+    uint64_t flush_done[2];
+    uint32_t tslot;
+    int bad;
+    int issued;     // stages whose MMAs have been issued
+};
+
+__device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
+    sy->bad = 1;
+    if (slots) slots[S_TC_TIMEOUT] = 1.0;
+}
+
+// After a timeout: wait (bounded) until the MMAs of the last two stages have
+// completed, so that TMEM is not released under an MMA in flight.
+__device__ __forceinline__ void drain(Sync* sy, int ns) {
+    __syncthreads();
+    const int n = sy->issued;
+    if (!sy->bad || n == 0) return;
+    for (int s = (n >= 2 ? n - 2 : 0); s < n; ++s)
+        mbar_wait(&sy->mma_done[s & 1], (s >> 1) & 1, TC_BUDGET);
+}
+
+// TMEM window flush: this thread's lane, columns [col0, col0 + HALF) of the
+// accumulator at column base dcol, folded into (acc, comp) with Kahan summation.
+template <int HALF>
+__device__ __forceinline__ void flush_window(uint32_t tmem, int lane_base, int dcol, int col0, float* acc, float* comp) {
+#pragma unroll
+    for (int c = 0; c < HALF / 8; ++c) {
+        float v[8];
+        tmem_ld8(tmem + ((uint32_t)lane_base << 16) + (uint32_t)(dcol + col0 + 8 * c), v);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const float y = v[t] - comp[8 * c + t];
+            const float s = acc[8 * c + t] + y;
+            comp[8 * c + t] = (s - acc[8 * c + t]) - y;
+            acc[8 * c + t] = s;
+        }
+    }
+}
+
+// Issues the 3 split products of one 64-deep stage into D (TMEM cols dcol..) for
+// the Hessian (N = NHP) and the gradient (N = 16).  A tiles: W_hi, W_lo, U_hi,
+// U_lo at aBase + t*aStride; B tiles: hi at bBase, lo at bBase + B_TILE.
+template <int K>
+__device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aBase, int aStride, int aLBO, int aSBO,
+                                            uint32_t bBase, bool first) {
+    using D = TcDims<K>;
+    constexpr uint32_t idH = idesc_bf16(D::NHP);
+    constexpr uint32_t idG = idesc_f16(D::NG);
+    const uint32_t dH = tmem + dcol;
+    const uint32_t dG = tmem + dcol + D::NHP;
+    const uint32_t bPPh = bBase, bPPl = bBase + D::B_TILE;
+    const uint32_t bPh = bBase + (D::NHP / 8) * SBO_STD, bPl = bPh + D::B_TILE;
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+        const uint32_t ao = ks * 2 * aLBO, bo = ks * 2 * LBO_STD;
+        const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
+        const uint64_t aWh = sdesc(aBase + ao, aLBO, aSBO), aWl = sdesc(aBase + aStride + ao, aLBO, aSBO);
+        const uint64_t aUh = sdesc(aBase + 2 * aStride + ao, aLBO, aSBO), aUl = sdesc(aBase + 3 * aStride + ao, aLBO, aSBO);
+        mma_bf16(dH, aWh, sdesc(bPPh + bo, LBO_STD, SBO_STD), idH, acc0);
+        mma_bf16(dH, aWh, sdesc(bPPl + bo, LBO_STD, SBO_STD), idH, 1u);
+        mma_bf16(dH, aWl, sdesc(bPPh + bo, LBO_STD, SBO_STD), idH, 1u);
+        mma_bf16(dG, aUh, sdesc(bPh + bo, LBO_STD, SBO_STD), idG, acc0);
+        mma_bf16(dG, aUh, sdesc(bPl + bo, LBO_STD, SBO_STD), idG, 1u);
+        mma_bf16(dG, aUl, sdesc(bPh + bo, LBO_STD, SBO_STD), idG, 1u);
+    }
+}
+
+// B tile item: row n (PP column for n < NHP, P column for n >= NHP), 8
+// consecutive reduction indices whose K-vectors start at vec[e * stride].
+template <int K>
+__device__ __forceinline__ void b_item(const float* vec0, int stride, int n, uint32_t dst_hi, uint32_t dst_lo) {
+    using D = TcDims<K>;
+    float v[8];
+    if (n < D::NHP) {
+        if (n < D::NH) {
+            int k, k2;
+            tri_pair<K>(n, k, k2);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = vec0[e * stride + k] * vec0[e * stride + k2];
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = 0.f;
+        }
+    } else {
+        const int kk = n - D::NHP;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) v[e] = kk < K ? vec0[e * stride + kk] * GB_SCALE : 0.f;
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split2_f16(v[2 * e], v[2 * e + 1], h[e], l[e]);
+        sts128(dst_hi, h[0], h[1], h[2], h[3]);
+        sts128(dst_lo, l[0], l[1], l[2], l[3]);
+        return;
+    }
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) split2(v[2 * e], v[2 * e + 1], h[e], l[e]);
+    sts128(dst_hi, h[0], h[1], h[2], h[3]);
+    sts128(dst_lo, l[0], l[1], l[2], l[3]);
+}
+
+// ------------------------------------------------------------------ Q side
+template <int K>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_accum_q_tc(PassArgs a) {
+    using D = TcDims<K>;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_STD]
+    const uint32_t sB = sA + 2 * 4 * A_TILE_STD;                     // [2][2][B_TILE]
+    float* P32 = (float*)(smem + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE);   // [2][64 * K]
+    Sync* sy = (Sync*)(P32 + 2 * 64 * K);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r = tid & 127, hf = tid >> 7;
+    const int64_t i = (int64_t)blockIdx.x * 128 + r;
+    const bool active = i < a.I;
+    const int w0 = blockIdx.y * a.per_chunk;
+    const int w1 = min(a.JW, w0 + a.per_chunk);
+    const int ns = (w1 - w0 + 1) / 2;
+
+    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+    if (tid == 0) {
+        mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
+        mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
+        sy->bad = 0;
+        sy->issued = 0;
+        mbar_fence_init();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sy->tslot;
+
+    float qi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) qi[k] = active ? (float)a.q[(int64_t)K * i + k] : 1.f / K;
+    float acc[D::HALF], comp[D::HALF];
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) { acc[c] = 0.f; comp[c] = 0.f; }
+    const int lane_base = 32 * (warp & 3);
+    const int col0 = hf * D::HALF;
+
+    for (int s = 0; s < ns; ++s) {
+        const int b = s & 1;
+        if (s >= 2 && !sy->bad) {
+            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        }
+        // stage p of blocks [jb, jb + 16) as fp32
+        const int64_t jb = 8 * (int64_t)(w0 + 2 * s);
+        float* P = P32 + b * 64 * K;
+        const int64_t base = jb * 4 * K, limit = a.J * 4 * K;
+        for (int t = tid; t < 64 * K; t += TC_THREADS) P[t] = (base + t < limit) ? (float)a.p[base + t] : 0.25f;
+        __syncthreads();
+        if (sy->bad) break;
+        // B tiles: NT rows x 8 groups of 8 columns m
+        const uint32_t bB = sB + b * 2 * D::B_TILE;
+        for (int it = tid; it < D::NT * 8; it += TC_THREADS) {
+            const int n = it % D::NT, kg = it / D::NT;
+            const uint32_t off = (n >> 3) * SBO_STD + kg * LBO_STD + (n & 7) * 16;
+            b_item<K>(P + kg * 8 * K, K, n, bB + off, bB + D::B_TILE + off);
+        }
+        // A tiles: this thread's row r, blocks hf*8 .. hf*8+7 of the stage
+        const int wd = w0 + 2 * s + hf;
+        const uint32_t word = (wd < w1) ? a.G[(int64_t)wd * a.Ipad + i] : HX_PAD_WORD;
+        const uint32_t aB = sA + b * 4 * A_TILE_STD;
+#pragma unroll 1
+        for (int t2 = 0; t2 < 4; ++t2) {
+            float W[8], U[8];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int bb = 2 * t2 + e;
+                const unsigned nib = (word >> (4 * bb)) & 0xFu;
+                const float* pb = P + (hf * 8 + bb) * 4 * K;
+                float qp[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    float sm = 0.f;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) sm = fmaf(qi[k], pb[h * K + k], sm);
+                    qp[h] = sm;
+                }
+                float L, u[4];
+                pair_eval<float>(nib, qp, L, u);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    U[4 * e + h] = u[h] * U_SCALE;
+                    W[4 * e + h] = u[h] * rcp_approx(qp[h]);
+                }
+            }
+            const uint32_t off = (r >> 3) * SBO_STD + (hf * 4 + t2) * LBO_STD + (r & 7) * 16;
+            uint32_t wh[4], wl[4], uh[4], ul[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                split2(W[2 * e], W[2 * e + 1], wh[e], wl[e]);
+                split2_f16(U[2 * e], U[2 * e + 1], uh[e], ul[e]);
+            }
+            sts128(aB + off, wh[0], wh[1], wh[2], wh[3]);
+            sts128(aB + A_TILE_STD + off, wl[0], wl[1], wl[2], wl[3]);
+            sts128(aB + 2 * A_TILE_STD + off, uh[0], uh[1], uh[2], uh[3]);
+            sts128(aB + 3 * A_TILE_STD + off, ul[0], ul[1], ul[2], ul[3]);
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        const int win = s / TC_FLUSH;
+        const int d = win & 1;
+        if (tid == 0) {
+            fence_after();
+            issue_stage<K>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, bB, (s % TC_FLUSH) == 0);
+            commit(&sy->mma_done[b]);
+            if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
+            sy->issued = s + 1;
+        }
+        // fold the previous window while the tensor core runs this stage
+        if ((s % TC_FLUSH) == 0 && s > 0) {
+            const int wp = win - 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
+            if (!ok) set_bad(sy, a.slots);
+            else {
+                fence_after();
+                flush_window<D::HALF>(tmem, lane_base, (wp & 1) * D::NT, col0, acc, comp);
+            }
+            fence_before();
+        }
+    }
+    // last window
+    __syncthreads();
+    if (ns > 0 && !sy->bad) {
+        const int wl = (ns - 1) / TC_FLUSH;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wl & 1], (wl >> 1) & 1, TC_BUDGET));
+        if (!ok) set_bad(sy, a.slots);
+        else {
+            fence_after();
+            flush_window<D::HALF>(tmem, lane_base, (wl & 1) * D::NT, col0, acc, comp);
+        }
+    }
+    drain(sy, ns);
+    fence_before();
+    __syncthreads();
+    // write partials: v < K gradient, v = K + tri index Hessian
+    constexpr int NV = K + D::NH;
+    double* out = a.part + (int64_t)blockIdx.y * NV * a.Ipad;
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) {
+        const int col = col0 + c;
+        const double val = (double)acc[c] - (double)comp[c];
+        if (col < D::NH) out[(int64_t)(K + col) * a.Ipad + i] = val;
+        else if (col >= D::NHP && col < D::NHP + K) out[(int64_t)(col - D::NHP) * a.Ipad + i] = val * G_UNSCALE;
+    }
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc<D::TCOLS>(tmem);
+    }
+}
+
+// ------------------------------------------------------------------ P side
+template <int K>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_accum_p_tc(PassArgs a) {
+    using D = TcDims<K>;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_PAD]
+    const uint32_t sB = sA + 2 * 4 * A_TILE_PAD;                     // [2][2][B_TILE]
+    float* Q32 = (float*)(smem + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE);   // [2][64 * K]
+    uint32_t* SW = (uint32_t*)(Q32 + 2 * 64 * K);                    // [2][4][64]
+    Sync* sy = (Sync*)(SW + 2 * 4 * 64);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int jl = tid >> 3, ig = tid & 7;
+    const int64_t j = (int64_t)blockIdx.x * 32 + jl;
+    const bool valid = j < a.J;
+    const int64_t i0 = (int64_t)blockIdx.y * a.per_chunk;
+    const int64_t i1 = min(a.I, i0 + (int64_t)a.per_chunk);
+    const int ns = (int)((i1 - i0 + 63) / 64);
+
+    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+    if (tid == 0) {
+        mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
+        mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
+        sy->bad = 0;
+        sy->issued = 0;
+        mbar_fence_init();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sy->tslot;
+
+    float pr[4][K];
+#pragma unroll
+    for (int h = 0; h < 4; ++h)
+#pragma unroll
+        for (int k = 0; k < K; ++k) pr[h][k] = valid ? (float)a.p[(int64_t)K * (4 * j + h) + k] : 0.25f;
+    float acc[D::HALF], comp[D::HALF];
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) { acc[c] = 0.f; comp[c] = 0.f; }
+    const int r = tid & 127, hf = tid >> 7;
+    const int lane_base = 32 * (warp & 3);
+    const int col0 = hf * D::HALF;
+    const int bsh = 4 * (jl & 7);
+
+    for (int s = 0; s < ns; ++s) {
+        const int b = s & 1;
+        if (s >= 2 && !sy->bad) {
+            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        }
+        const int64_t is = i0 + 64 * (int64_t)s;
+        const int n = (int)min((int64_t)64, i1 - is);
+        float* Qs = Q32 + b * 64 * K;
+        uint32_t* Ws = SW + b * 4 * 64;
+        for (int t = tid; t < 64 * K; t += TC_THREADS) Qs[t] = (t < n * K) ? (float)a.q[(int64_t)K * is + t] : 1.f / K;
+        {
+            const int w = tid >> 6, ii = tid & 63;
+            const int64_t jw = (int64_t)blockIdx.x * 4 + w;
+            Ws[tid] = (ii < n && jw < a.JW) ? a.G[jw * a.Ipad + is + ii] : HX_PAD_WORD;
+        }
+        __syncthreads();
+        if (sy->bad) break;
+        const uint32_t bB = sB + b * 2 * D::B_TILE;
+        for (int it = tid; it < D::NT * 8; it += TC_THREADS) {
+            const int nn = it % D::NT, kg = it / D::NT;
+            const uint32_t off = (nn >> 3) * SBO_STD + kg * LBO_STD + (nn & 7) * 16;
+            b_item<K>(Qs + kg * 8 * K, K, nn, bB + off, bB + D::B_TILE + off);
+        }
+        // A = W^T tile: rows m = 4*jl + h, reduction over the stage's 64 individuals
+        float W[4][8], U[4][8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int ii = ig * 8 + e;
+            const unsigned nib = (Ws[(jl >> 3) * 64 + ii] >> bsh) & 0xFu;
+            const float* qr = Qs + ii * K;
+            float qv[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) qv[k] = qr[k];
+            float qp[4];
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                float sm = 0.f;
+#pragma unroll
+                for (int k = 0; k < K; ++k) sm = fmaf(qv[k], pr[h][k], sm);
+                qp[h] = sm;
+            }
+            float L, u[4];
+            pair_eval<float>(nib, qp, L, u);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                U[h][e] = u[h] * U_SCALE;
+                W[h][e] = u[h] * rcp_approx(qp[h]);
+            }
+        }
+        const uint32_t aB = sA + b * 4 * A_TILE_PAD;
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int m = 4 * jl + h;
+            const uint32_t off = (m >> 3) * SBO_PAD + ig * LBO_PAD + (m & 7) * 16;
+            uint32_t wh[4], wl[4], uh[4], ul[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                split2(W[h][2 * e], W[h][2 * e + 1], wh[e], wl[e]);
+                split2_f16(U[h][2 * e], U[h][2 * e + 1], uh[e], ul[e]);
+            }
+            sts128(aB + off, wh[0], wh[1], wh[2], wh[3]);
+            sts128(aB + A_TILE_PAD + off, wl[0], wl[1], wl[2], wl[3]);
+            sts128(aB + 2 * A_TILE_PAD + off, uh[0], uh[1], uh[2], uh[3]);
+            sts128(aB + 3 * A_TILE_PAD + off, ul[0], ul[1], ul[2], ul[3]);
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        const int win = s / TC_FLUSH;
+        const int d = win & 1;
+        if (tid == 0) {
+            fence_after();
+            issue_stage<K>(tmem, d * D::NT, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, bB, (s % TC_FLUSH) == 0);
+            commit(&sy->mma_done[b]);
+            if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
+            sy->issued = s + 1;
+        }
+        if ((s % TC_FLUSH) == 0 && s > 0) {
+            const int wp = win - 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
+            if (!ok) set_bad(sy, a.slots);
+            else {
+                fence_after();
+                flush_window<D::HALF>(tmem, lane_base, (wp & 1) * D::NT, col0, acc, comp);
+            }
+            fence_before();
+        }
+    }
+    __syncthreads();
+    if (ns > 0 && !sy->bad) {
+        const int wl = (ns - 1) / TC_FLUSH;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wl & 1], (wl >> 1) & 1, TC_BUDGET));
+        if (!ok) set_bad(sy, a.slots);
+        else {
+            fence_after();
+            flush_window<D::HALF>(tmem, lane_base, (wl & 1) * D::NT, col0, acc, comp);
+        }
+    }
+    drain(sy, ns);
+    fence_before();
+    __syncthreads();
+    // rows m of this CTA: TMEM lane r
+    const int64_t m = (int64_t)blockIdx.x * 128 + r;
+    if (m < 4 * a.J) {
+        constexpr int NV = K + D::NH;
+#pragma unroll
+        for (int c = 0; c < D::HALF; ++c) {
+            const int col = col0 + c;
+            const double val = (double)acc[c] - (double)comp[c];
+            if (a.S == 1) {
+                if (col < D::NH) {
+                    int k, k2;
+                    tri_pair<K>(col, k, k2);
+                    a.XtX[(int64_t)K * K * m + k2 + K * k] = val;
+                    a.XtX[(int64_t)K * K * m + k + K * k2] = val;
+                } else if (col >= D::NHP && col < D::NHP + K) {
+                    a.Xtz[(int64_t)K * m + (col - D::NHP)] = val * G_UNSCALE;
+                }
+            } else {
+                const int64_t rows = 4 * a.J;
+                double* out = a.part + (int64_t)blockIdx.y * NV * rows;
+                if (col < D::NH) out[(int64_t)(K + col) * rows + m] = val;
+                else if (col >= D::NHP && col < D::NHP + K) out[(int64_t)(col - D::NHP) * rows + m] = val * G_UNSCALE;
+            }
+        }
+    }
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc<D::TCOLS>(tmem);
+    }
+}
+
+template <int K> constexpr size_t smem_q() {
+    using D = TcDims<K>;
+    return 1024 + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE + 2 * 64 * K * 4 + sizeof(Sync);
+}
+template <int K> constexpr size_t smem_p() {
+    using D = TcDims<K>;
+    return 1024 + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE + 2 * 64 * K * 4 + 2 * 4 * 64 * 4 + sizeof(Sync);
+}
+
+#define HX_FOR_K(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
+
+}  // namespace
+
+cudaError_t init_tc_attrs() {
+    cudaError_t e = cudaSuccess;
+#define HX_ATTR(KK)                                                                                   \
+    if (e == cudaSuccess)                                                                             \
+        e = cudaFuncSetAttribute(k_accum_q_tc<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                                 (int)smem_q<KK>());                                                  \
+    if (e == cudaSuccess)                                                                             \
+        e = cudaFuncSetAttribute(k_accum_p_tc<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                                 (int)smem_p<KK>());
+    HX_FOR_K(HX_ATTR)
+#undef HX_ATTR
+    return e;
+}
+
+cudaError_t launch_accum_q_tc(int K, const PassArgs& a, cudaStream_t st) {
+    dim3 grid((unsigned)(a.Ipad / 128), (unsigned)a.S);
+#define HX_CASE(KK) case KK: k_accum_q_tc<KK><<<grid, TC_THREADS, smem_q<KK>(), st>>>(a); break;
+    switch (K) { HX_FOR_K(HX_CASE) default: return cudaErrorInvalidValue; }
+#undef HX_CASE
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accum_p_tc(int K, const PassArgs& a, cudaStream_t st) {
+    dim3 grid((unsigned)((a.J + 31) / 32), (unsigned)a.S);
+#define HX_CASE(KK) case KK: k_accum_p_tc<KK><<<grid, TC_THREADS, smem_p<KK>(), st>>>(a); break;
+    switch (K) { HX_FOR_K(HX_CASE) default: return cudaErrorInvalidValue; }
+#undef HX_CASE
+    return cudaGetLastError();
+}
+
+}  // namespace hx

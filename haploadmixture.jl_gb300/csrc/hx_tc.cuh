@@ -1,0 +1,127 @@
+// hx_tc.cuh -- tcgen05 (5th-generation tensor core) building blocks for sm_103a.
+//
+// Operands live in shared memory in the canonical no-swizzle K-major layout:
+// 8-row x 16-byte core matrices; element (row r, reduction index k) of a bf16
+// tile sits at (r/8)*SBO + (k/8)*LBO + (r%8)*16 + (k%8)*2.  Accumulators live
+// in tensor memory (TMEM): row r of an M=128 tile is TMEM lane r, column n is
+// one 32-bit TMEM column.  All waits are bounded: on timeout a kernel records
+// an error and leaves its loops without touching results.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hx {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading (K-direction)
+// and stride (M/N-direction) byte offsets, fixed version bits 46-48 = 0b001,
+// base offset 0, relative LBO mode, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 accumulator, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16(int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
+}
+// Same with IEEE FP16 A and B.
+__host__ __device__ constexpr uint32_t idesc_f16(int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile("{ .reg .pred p; setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
+                 :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void commit(uint64_t* mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(smem_u32(mbar)) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(m)), "r"(count));
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, long long budget_cycles) {
+    const uint32_t addr = smem_u32(m);
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+        if (done) return true;
+        if (clock64() - t0 > budget_cycles) return false;
+    }
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(slot)), "n"(NCOLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+template <int NCOLS>
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "n"(NCOLS));
+}
+
+// 8 consecutive 32-bit TMEM columns of this thread's lane (warp w reads lanes 32*(w%4)..+31).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int t = 0; t < 8; ++t) v[t] = __uint_as_float(r[t]);
+}
+
+// x ~= hi + lo with hi, lo bf16 (round to nearest even); returns packed pairs
+// for two values: hi2 = {hi(x0) low half, hi(x1) high half}, lo2 likewise.
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi2, uint32_t& lo2) {
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hi2) : "f"(x1), "f"(x0));
+    const float h0 = __uint_as_float(hi2 << 16);
+    const float h1 = __uint_as_float(hi2 & 0xFFFF0000u);
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(lo2) : "f"(x1 - h1), "f"(x0 - h0));
+}
+
+// The same split in IEEE FP16 (11 significant bits per part).
+__device__ __forceinline__ void split2_f16(float x0, float x1, uint32_t& hi2, uint32_t& lo2) {
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(hi2) : "f"(x1), "f"(x0));
+    float h0, h1;
+    asm("{ .reg .b16 a, b; mov.b32 {a, b}, %2; cvt.f32.f16 %0, a; cvt.f32.f16 %1, b; }"
+        : "=f"(h0), "=f"(h1) : "r"(hi2));
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(lo2) : "f"(x1 - h1), "f"(x0 - h0));
+}
+
+__device__ __forceinline__ void sts128(uint32_t saddr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" :: "r"(saddr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Upper-triangle index of (k, k2), k <= k2, and its inverse.
+template <int K> __host__ __device__ constexpr int tri_idx(int k, int k2) { return k * K - (k * (k - 1)) / 2 + (k2 - k); }
+template <int K> __device__ __forceinline__ void tri_pair(int c, int& k, int& k2) {
+    int kk = 0;
+#pragma unroll
+    for (int t = 0; t < K; ++t)
+        if (c >= tri_idx<K>(t, t)) kk = t;
+    k = kk;
+    k2 = kk + (c - tri_idx<K>(kk, kk));
+}
+
+}  // namespace tc
+}  // namespace hx

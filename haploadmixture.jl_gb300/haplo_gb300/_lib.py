@@ -16,11 +16,13 @@ HX_KMAX = 12
 HX_QMAX = 6
 HX_PREC_FP64 = 0
 HX_PREC_MIXED = 1
+HX_PATH_AUTO = 0
+HX_PATH_CUDA_CORES = 1
 
 
 class HxOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("Qsec", C.c_int32), ("verbose", C.c_int32),
-                ("rho", C.c_double), ("pseudocount", C.c_double)]
+                ("rho", C.c_double), ("pseudocount", C.c_double), ("path", C.c_int32), ("reserved", C.c_int32)]
 
 
 class HxIterInfo(C.Structure):

@@ -37,7 +37,7 @@ class GB300Admix:
     """
 
     def __init__(self, bed, I, J, K, *, bytes_per_snp=None, n_snp=None, precision="fp64", Q=3, device=0,
-                 rho=1e7, pseudocount=1e-5, verbose=False, bed_on_device=False):
+                 rho=1e7, pseudocount=1e-5, verbose=False, bed_on_device=False, path="auto"):
         lib = _lib.load()
         self.I, self.J, self.K = int(I), int(J), int(K)
         opts = _lib.HxOpts()
@@ -48,6 +48,7 @@ class GB300Admix:
         opts.verbose = 1 if verbose else 0
         opts.rho = rho
         opts.pseudocount = pseudocount
+        opts.path = {"auto": _lib.HX_PATH_AUTO, "cuda_cores": _lib.HX_PATH_CUDA_CORES}[path]
         self.precision = precision
         self.Q = Q
         h = C.c_void_p()

@@ -47,6 +47,9 @@ extern "C" {
 
 typedef struct hx_ctx hx_ctx;
 
+#define HX_PATH_AUTO 0     /* mixed method: Hessian passes on the tensor cores (tcgen05) */
+#define HX_PATH_CUDA_CORES 1  /* mixed method: every pass on the CUDA cores */
+
 typedef struct hx_opts {
     int32_t precision;     /* HX_PREC_FP64 (default) or HX_PREC_MIXED */
     int32_t device;        /* CUDA device ordinal (default 0) */
@@ -54,6 +57,8 @@ typedef struct hx_opts {
     int32_t verbose;       /* 1: one JSON line per outer iteration on stderr */
     double rho;            /* P-step penalty (default 1e7; algorithms_inner.jl:225) */
     double pseudocount;    /* projection floor (default 1e-5; utils.jl:20) */
+    int32_t path;          /* HX_PATH_AUTO (default) or HX_PATH_CUDA_CORES */
+    int32_t reserved;
 } hx_opts;
 
 typedef struct hx_iter_info {
