@@ -130,18 +130,17 @@ void plan(hx_ctx* c) {
     ipc = (ipc + PSTAGE_IND - 1) / PSTAGE_IND * PSTAGE_IND;
     c->ipc_p = (int)ipc;
     c->S_p = (int)((c->I + ipc - 1) / ipc);
-    // tensor-core passes: one 256-thread CTA per SM; aim for >= 8 waves of 152
-    const int64_t target_tc = 8 * 152;
+    // tensor-core passes: two 256-thread CTAs per SM; aim for >= 8 waves of 2 x 152
+    const int64_t target_tc = 8 * 2 * 152;
     int64_t St = std::max<int64_t>(1, (target_tc + tilesQ - 1) / tilesQ);
-    St = std::min<int64_t>(St, (c->JW + 1) / 2);
-    int64_t wpc = (c->JW + St - 1) / St;
-    wpc = (wpc + 1) / 2 * 2;                 // whole stages of 2 words (16 blocks)
+    St = std::min<int64_t>(St, c->JW);
+    int64_t wpc = (c->JW + St - 1) / St;     // stages of one word (8 blocks)
     c->wpc_qt = (int)wpc;
     c->S_qt = (int)((c->JW + wpc - 1) / wpc);
     int64_t Spt = std::max<int64_t>(1, (target_tc + tilesP - 1) / tilesP);
-    Spt = std::min<int64_t>(Spt, (c->I + 63) / 64);
+    Spt = std::min<int64_t>(Spt, (c->I + 31) / 32);
     int64_t ipt = (c->I + Spt - 1) / Spt;
-    ipt = (ipt + 63) / 64 * 64;              // whole stages of 64 individuals
+    ipt = (ipt + 31) / 32 * 32;              // whole stages of 32 individuals
     c->ipc_pt = (int)ipt;
     c->S_pt = (int)((c->I + ipt - 1) / ipt);
 }

@@ -6,20 +6,24 @@
 //   P side (src/loops.jl:367-403):  H_m = sum_i W[i,m] QQ[i,:],  g_m = sum_i U[i,m] Q[i,:]
 // with m = 4j+h, U = c_h/qp_h, W = c_h/qp_h^2, PP[m,(k,k2)] = p[k,m] p[k2,m]
 // (upper triangle) and QQ[i,(k,k2)] = q[k,i] q[k2,i].  The CUDA cores evaluate
-// each (individual, block) pair once (qp, class, U, W) and write bf16 hi/lo
+// each (individual, block) pair once (qp, class, U, W) and write 16-bit hi/lo
 // splits of U and W into shared memory; one thread issues
-// tcgen05.mma kind::f16 (bf16 x bf16 -> fp32 in TMEM) for hi*hi + hi*lo + lo*hi.
+// tcgen05.mma kind::f16 (16-bit x 16-bit -> fp32 in TMEM) for hi*hi + hi*lo + lo*hi.
 // The Hessian operands use BF16 (8-bit exponent) because W spans ~1 .. 2e10,
 // beyond FP16's range: hi+lo carries 16 significant bits.  The gradient
 // operands use IEEE FP16 hi/lo (22 bits) under exact power-of-two scaling,
-// since the gradient fixes the optimum and the Hessian only the step.  TMEM accumulates FP32 over windows of TC_FLUSH
-// stages; each window is folded into registers (FP32, Kahan-compensated), and
-// chunk partials are summed in FP64 by the same reduction as the CUDA-core pass.
+// since the gradient fixes the optimum and the Hessian only the step.
+// TMEM accumulates FP32 over windows of TC_FLUSH stages; each window is folded
+// into registers (the gradient Kahan-compensated), and chunk partials are
+// summed in FP64 by the same reduction as the CUDA-core pass.
 //
-// Pipeline per stage: [wait MMA of stage s-2 done] -> stage inputs -> generate
-// A and B tiles (double-buffered) -> barrier -> one thread issues the MMAs and
-// commits to an mbarrier -> the previous TMEM window is flushed while the
-// tensor core works.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
+// Pipeline per stage (32 reduction indices): the next stage's global inputs
+// are prefetched into registers; [wait MMA of stage s-2] -> stage inputs to
+// shared memory -> generate A and B tiles (double-buffered) -> barrier -> one
+// thread issues the MMAs and commits to an mbarrier -> the previous TMEM window
+// is folded while the tensor core runs.  ~100 KB of shared memory per CTA, so
+// two CTAs (16 warps) share an SM and cover each other's barrier and load
+// stalls.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
 // slots[S_TC_TIMEOUT] and the CTA drains and exits.
 #include "hx_ops.cuh"
 #include "hx_tc.cuh"
@@ -29,17 +33,18 @@ namespace {
 using namespace tc;
 
 constexpr int TC_THREADS = 256;
-constexpr int TC_FLUSH = 4;
+constexpr int TC_FLUSH = 8;                // stages per TMEM window (256 reduction indices)
 constexpr long long TC_BUDGET = 4000000000LL;
-constexpr int SBO_STD = 1024;     // 8 core matrices (64 reduction elements) per row group
+constexpr int KD = 32;                     // reduction indices per stage
 constexpr int LBO_STD = 128;
-constexpr int LBO_PAD = 144;      // P-side A: padded so the generator stores are bank-conflict free
-constexpr int SBO_PAD = 8 * LBO_PAD;
-constexpr int A_TILE_STD = 16 * SBO_STD;   // 128 rows x 64 bf16
+constexpr int SBO_STD = (KD / 8) * LBO_STD;      // 512
+constexpr int LBO_PAD = 144;               // P-side A: padded for conflict-free generator stores
+constexpr int SBO_PAD = (KD / 8) * LBO_PAD;      // 576
+constexpr int A_TILE_STD = 16 * SBO_STD;   // 128 rows x 32 x 2 B = 8 KB
 constexpr int A_TILE_PAD = 16 * SBO_PAD;
-// Gradient operands use IEEE FP16 hi/lo (22 significant bits) under exact
-// power-of-two scaling that keeps them in FP16's normal range:
-// U * 2^-2 <= 5e4 (U = c/qp <= 2/1e-5), P or Q * 2^12 in [0.04, 4096].
+// Gradient operands: IEEE FP16 hi/lo under exact power-of-two scaling that keeps
+// them in FP16's normal range: U * 2^-2 <= 5e4 (U = c/qp <= 2/1e-5); P or Q * 2^12
+// in [0.04, 4096].
 constexpr float U_SCALE = 0.25f;
 constexpr float GB_SCALE = 4096.0f;
 constexpr double G_UNSCALE = 1.0 / 1024.0;
@@ -51,7 +56,10 @@ template <int K> struct TcDims {
     static constexpr int NT = NHP + NG;
     static constexpr int TCOLS = (2 * NT <= 32) ? 32 : (2 * NT <= 64) ? 64 : (2 * NT <= 128) ? 128 : 256;
     static constexpr int HALF = NT / 2;
-    static constexpr int B_TILE = NT * 128;    // NT rows x 64 bf16
+    static constexpr int B_TILE = (NT / 8) * SBO_STD;    // NT rows x 32 x 2 B
+    static constexpr int VPT = (KD * K + TC_THREADS - 1) / TC_THREADS;   // staged values per thread
+    // CTAs per SM: 2 while the generators fit in 128 registers, else 1
+    static constexpr int MINB = K <= 8 ? 2 : 1;
 };
 
 struct Sync {
@@ -67,37 +75,58 @@ __device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
     if (slots) slots[S_TC_TIMEOUT] = 1.0;
 }
 
-// After a timeout: wait (bounded) until the MMAs of the last two stages have
-// completed, so that TMEM is not released under an MMA in flight.
-__device__ __forceinline__ void drain(Sync* sy, int ns) {
+// After a timeout: wait (bounded) until the MMAs of the last two issued stages
+// have completed, so that TMEM is not released under an MMA in flight.
+__device__ __forceinline__ void drain(Sync* sy) {
     __syncthreads();
     const int n = sy->issued;
     if (!sy->bad || n == 0) return;
-    for (int s = (n >= 2 ? n - 2 : 0); s < n; ++s)
-        mbar_wait(&sy->mma_done[s & 1], (s >> 1) & 1, TC_BUDGET);
+    for (int s = (n >= 2 ? n - 2 : 0); s < n; ++s) mbar_wait(&sy->mma_done[s & 1], (s >> 1) & 1, TC_BUDGET);
 }
 
-// TMEM window flush: this thread's lane, columns [col0, col0 + HALF) of the
-// accumulator at column base dcol, folded into (acc, comp) with Kahan summation.
-template <int HALF>
-__device__ __forceinline__ void flush_window(uint32_t tmem, int lane_base, int dcol, int col0, float* acc, float* comp) {
+// TMEM window fold: this thread's lane, columns [HF*HALF, HF*HALF + HALF) of the
+// accumulator at column base dcol.  Hessian columns add plainly; gradient
+// columns (>= NHP) use Kahan compensation in comp[col - NHP].
+template <int K, int HF>
+__device__ __forceinline__ void fold(uint32_t taddr_lane, int dcol, float* acc, float* comp) {
+    using D = TcDims<K>;
 #pragma unroll
-    for (int c = 0; c < HALF / 8; ++c) {
+    for (int c = 0; c < D::HALF / 8; ++c) {
         float v[8];
-        tmem_ld8(tmem + ((uint32_t)lane_base << 16) + (uint32_t)(dcol + col0 + 8 * c), v);
+        tmem_ld8(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), v);
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
-            const float y = v[t] - comp[8 * c + t];
-            const float s = acc[8 * c + t] + y;
-            comp[8 * c + t] = (s - acc[8 * c + t]) - y;
-            acc[8 * c + t] = s;
+            const int col = HF * D::HALF + 8 * c + t;
+            if (col >= D::NHP) {
+                const float y = v[t] - comp[col - D::NHP];
+                const float s = acc[8 * c + t] + y;
+                comp[col - D::NHP] = (s - acc[8 * c + t]) - y;
+                acc[8 * c + t] = s;
+            } else {
+                acc[8 * c + t] += v[t];
+            }
         }
     }
 }
+template <int K>
+__device__ __forceinline__ void fold_half(int hf, uint32_t taddr_lane, int dcol, float* acc, float* comp) {
+    if (hf == 0) fold<K, 0>(taddr_lane, dcol, acc, comp);
+    else fold<K, 1>(taddr_lane, dcol, acc, comp);
+}
+// Applies the Kahan compensation to the gradient columns: acc then holds the sums.
+template <int K, int HF>
+__device__ __forceinline__ void compensate(float* acc, const float* comp) {
+    using D = TcDims<K>;
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) {
+        const int col = HF * D::HALF + c;
+        if (col >= D::NHP) acc[c] -= comp[col - D::NHP];
+    }
+}
 
-// Issues the 3 split products of one 64-deep stage into D (TMEM cols dcol..) for
-// the Hessian (N = NHP) and the gradient (N = 16).  A tiles: W_hi, W_lo, U_hi,
-// U_lo at aBase + t*aStride; B tiles: hi at bBase, lo at bBase + B_TILE.
+// Issues the 3 split products of one 32-deep stage into D (TMEM cols dcol..):
+// Hessian (N = NHP, bf16) and gradient (N = 16, fp16).  A tiles W_hi, W_lo,
+// U_hi, U_lo at aBase + t*aStride; B tiles: hi at bBase, lo at bBase + B_TILE.
 template <int K>
 __device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aBase, int aStride, int aLBO, int aSBO,
                                             uint32_t bBase, bool first) {
@@ -109,7 +138,7 @@ __device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aB
     const uint32_t bPPh = bBase, bPPl = bBase + D::B_TILE;
     const uint32_t bPh = bBase + (D::NHP / 8) * SBO_STD, bPl = bPh + D::B_TILE;
 #pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
+    for (int ks = 0; ks < KD / 16; ++ks) {
         const uint32_t ao = ks * 2 * aLBO, bo = ks * 2 * LBO_STD;
         const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
         const uint64_t aWh = sdesc(aBase + ao, aLBO, aSBO), aWl = sdesc(aBase + aStride + ao, aLBO, aSBO);
@@ -123,60 +152,58 @@ __device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aB
     }
 }
 
-// B tile item: row n (PP column for n < NHP, P column for n >= NHP), 8
-// consecutive reduction indices whose K-vectors start at vec[e * stride].
+// B tile item: row n (PP column for n < NHP, P/Q column for n >= NHP), 8
+// consecutive reduction indices whose K-vectors start at vec0[e * K].
 template <int K>
-__device__ __forceinline__ void b_item(const float* vec0, int stride, int n, uint32_t dst_hi, uint32_t dst_lo) {
+__device__ __forceinline__ void b_item(const float* vec0, int n, uint32_t dst_hi, uint32_t dst_lo) {
     using D = TcDims<K>;
     float v[8];
-    if (n < D::NHP) {
+    uint32_t h[4], l[4];
+    if (n >= D::NHP) {
+        const int kk = n - D::NHP;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) v[e] = kk < K ? vec0[e * K + kk] * GB_SCALE : 0.f;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split2_f16(v[2 * e], v[2 * e + 1], h[e], l[e]);
+    } else {
         if (n < D::NH) {
             int k, k2;
             tri_pair<K>(n, k, k2);
 #pragma unroll
-            for (int e = 0; e < 8; ++e) v[e] = vec0[e * stride + k] * vec0[e * stride + k2];
+            for (int e = 0; e < 8; ++e) v[e] = vec0[e * K + k] * vec0[e * K + k2];
         } else {
 #pragma unroll
             for (int e = 0; e < 8; ++e) v[e] = 0.f;
         }
-    } else {
-        const int kk = n - D::NHP;
 #pragma unroll
-        for (int e = 0; e < 8; ++e) v[e] = kk < K ? vec0[e * stride + kk] * GB_SCALE : 0.f;
-        uint32_t h[4], l[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) split2_f16(v[2 * e], v[2 * e + 1], h[e], l[e]);
-        sts128(dst_hi, h[0], h[1], h[2], h[3]);
-        sts128(dst_lo, l[0], l[1], l[2], l[3]);
-        return;
+        for (int e = 0; e < 4; ++e) split2(v[2 * e], v[2 * e + 1], h[e], l[e]);
     }
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) split2(v[2 * e], v[2 * e + 1], h[e], l[e]);
     sts128(dst_hi, h[0], h[1], h[2], h[3]);
     sts128(dst_lo, l[0], l[1], l[2], l[3]);
 }
 
-// ------------------------------------------------------------------ Q side
+// One (individual, block) pair: qp from q and p (4K values), then U (scaled)
+// and W.
 template <int K>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_accum_q_tc(PassArgs a) {
-    using D = TcDims<K>;
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_STD]
-    const uint32_t sB = sA + 2 * 4 * A_TILE_STD;                     // [2][2][B_TILE]
-    float* P32 = (float*)(smem + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE);   // [2][64 * K]
-    Sync* sy = (Sync*)(P32 + 2 * 64 * K);
+__device__ __forceinline__ void gen_pair(unsigned nib, const float* qv, const float* pb, float* U4, float* W4) {
+    float qp[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        float sm = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) sm = fmaf(qv[k], pb[h * K + k], sm);
+        qp[h] = sm;
+    }
+    float L, u[4];
+    pair_eval<float>(nib, qp, L, u);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        U4[h] = u[h] * U_SCALE;
+        W4[h] = u[h] * rcp_approx(qp[h]);
+    }
+}
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int r = tid & 127, hf = tid >> 7;
-    const int64_t i = (int64_t)blockIdx.x * 128 + r;
-    const bool active = i < a.I;
-    const int w0 = blockIdx.y * a.per_chunk;
-    const int w1 = min(a.JW, w0 + a.per_chunk);
-    const int ns = (w1 - w0 + 1) / 2;
-
-    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+__device__ __forceinline__ void init_sync(Sync* sy, int tid) {
     if (tid == 0) {
         mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
         mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
@@ -184,68 +211,146 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_accum_q_tc(PassArgs a) {
         sy->issued = 0;
         mbar_fence_init();
     }
+}
+
+// Shared tail of the main loop: MMA issue for stage s and the fold of the
+// previous TMEM window.
+template <int K>
+__device__ __forceinline__ void issue_and_fold(Sync* sy, double* slots, int tid, int hf, int s, int ns, int b,
+                                               uint32_t tmem, uint32_t taddr_lane, uint32_t aB, int aStride, int aLBO,
+                                               int aSBO, uint32_t bB, float* acc, float* comp) {
+    using D = TcDims<K>;
+    const int win = s / TC_FLUSH;
+    const int d = win & 1;
+    if (tid == 0) {
+        fence_after();
+        issue_stage<K>(tmem, d * D::NT, aB, aStride, aLBO, aSBO, bB, (s % TC_FLUSH) == 0);
+        commit(&sy->mma_done[b]);
+        if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
+        sy->issued = s + 1;
+    }
+    if ((s % TC_FLUSH) == 0 && s > 0) {
+        const int wp = win - 1;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
+        if (!ok) set_bad(sy, slots);
+        else {
+            fence_after();
+            fold_half<K>(hf, taddr_lane, (wp & 1) * D::NT, acc, comp);
+        }
+        fence_before();
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int ns, uint32_t taddr_lane, float* acc,
+                                           float* comp) {
+    using D = TcDims<K>;
+    __syncthreads();
+    if (ns > 0 && !sy->bad) {
+        const int wl = (ns - 1) / TC_FLUSH;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wl & 1], (wl >> 1) & 1, TC_BUDGET));
+        if (!ok) set_bad(sy, slots);
+        else {
+            fence_after();
+            fold_half<K>(hf, taddr_lane, (wl & 1) * D::NT, acc, comp);
+        }
+    }
+    drain(sy);
+    fence_before();
+    __syncthreads();
+    if (hf == 0) compensate<K, 0>(acc, comp);
+    else compensate<K, 1>(acc, comp);
+}
+
+// ------------------------------------------------------------------ Q side
+// CTA: 128 individuals (TMEM lanes) x a chunk of class words; stage = 1 word
+// (8 blocks, 32 haplotype columns).  Thread (r, hf): row r, blocks 4hf..4hf+3.
+template <int K>
+__global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(PassArgs a) {
+    using D = TcDims<K>;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_STD]
+    const uint32_t sB = sA + 2 * 4 * A_TILE_STD;                     // [2][2][B_TILE]
+    float* P32 = (float*)(smem + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE);   // [2][KD * K]
+    Sync* sy = (Sync*)(P32 + 2 * KD * K);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = tid & 127, hf = tid >> 7;
+    const int64_t i = (int64_t)blockIdx.x * 128 + r;
+    const bool active = i < a.I;
+    const int w0 = blockIdx.y * a.per_chunk;
+    const int ns = min(a.JW, w0 + a.per_chunk) - w0;     // one word per stage
+    const int64_t plimit = a.J * 4 * K;
+
+    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+    init_sync(sy, tid);
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = sy->tslot;
+    const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
 
     float qi[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) qi[k] = active ? (float)a.q[(int64_t)K * i + k] : 1.f / K;
-    float acc[D::HALF], comp[D::HALF];
+    float acc[D::HALF], comp[D::NG];
 #pragma unroll
-    for (int c = 0; c < D::HALF; ++c) { acc[c] = 0.f; comp[c] = 0.f; }
-    const int lane_base = 32 * (warp & 3);
-    const int col0 = hf * D::HALF;
+    for (int c = 0; c < D::HALF; ++c) acc[c] = 0.f;
+#pragma unroll
+    for (int c = 0; c < D::NG; ++c) comp[c] = 0.f;
+
+    // prefetch registers for stage 0
+    uint32_t word_nx = (ns > 0) ? a.G[(int64_t)w0 * a.Ipad + i] : HX_PAD_WORD;
+    float pv_nx[D::VPT];
+#pragma unroll
+    for (int v = 0; v < D::VPT; ++v) {
+        const int t = tid + v * TC_THREADS;
+        const int64_t g = (int64_t)w0 * 8 * 4 * K + t;
+        pv_nx[v] = (t < KD * K && g < plimit) ? (float)a.p[g] : 0.25f;
+    }
 
     for (int s = 0; s < ns; ++s) {
         const int b = s & 1;
+        const uint32_t word = word_nx;
+        float* P = P32 + b * KD * K;
+        // buffer b was last read by the MMAs of stage s-2
         if (s >= 2 && !sy->bad) {
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         }
-        // stage p of blocks [jb, jb + 16) as fp32
-        const int64_t jb = 8 * (int64_t)(w0 + 2 * s);
-        float* P = P32 + b * 64 * K;
-        const int64_t base = jb * 4 * K, limit = a.J * 4 * K;
-        for (int t = tid; t < 64 * K; t += TC_THREADS) P[t] = (base + t < limit) ? (float)a.p[base + t] : 0.25f;
+#pragma unroll
+        for (int v = 0; v < D::VPT; ++v) {
+            const int t = tid + v * TC_THREADS;
+            if (t < KD * K) P[t] = pv_nx[v];
+        }
+        if (s + 1 < ns) {            // the next stage's loads, consumed next iteration
+            const int wn = w0 + s + 1;
+            word_nx = a.G[(int64_t)wn * a.Ipad + i];
+#pragma unroll
+            for (int v = 0; v < D::VPT; ++v) {
+                const int t = tid + v * TC_THREADS;
+                const int64_t g = (int64_t)wn * 8 * 4 * K + t;
+                pv_nx[v] = (t < KD * K && g < plimit) ? (float)a.p[g] : 0.25f;
+            }
+        }
         __syncthreads();
         if (sy->bad) break;
-        // B tiles: NT rows x 8 groups of 8 columns m
         const uint32_t bB = sB + b * 2 * D::B_TILE;
-        for (int it = tid; it < D::NT * 8; it += TC_THREADS) {
+        for (int it = tid; it < D::NT * (KD / 8); it += TC_THREADS) {
             const int n = it % D::NT, kg = it / D::NT;
             const uint32_t off = (n >> 3) * SBO_STD + kg * LBO_STD + (n & 7) * 16;
-            b_item<K>(P + kg * 8 * K, K, n, bB + off, bB + D::B_TILE + off);
+            b_item<K>(P + kg * 8 * K, n, bB + off, bB + D::B_TILE + off);
         }
-        // A tiles: this thread's row r, blocks hf*8 .. hf*8+7 of the stage
-        const int wd = w0 + 2 * s + hf;
-        const uint32_t word = (wd < w1) ? a.G[(int64_t)wd * a.Ipad + i] : HX_PAD_WORD;
         const uint32_t aB = sA + b * 4 * A_TILE_STD;
-#pragma unroll 1
-        for (int t2 = 0; t2 < 4; ++t2) {
+#pragma unroll
+        for (int t2 = 0; t2 < 2; ++t2) {
             float W[8], U[8];
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                const int bb = 2 * t2 + e;
-                const unsigned nib = (word >> (4 * bb)) & 0xFu;
-                const float* pb = P + (hf * 8 + bb) * 4 * K;
-                float qp[4];
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    float sm = 0.f;
-#pragma unroll
-                    for (int k = 0; k < K; ++k) sm = fmaf(qi[k], pb[h * K + k], sm);
-                    qp[h] = sm;
-                }
-                float L, u[4];
-                pair_eval<float>(nib, qp, L, u);
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    U[4 * e + h] = u[h] * U_SCALE;
-                    W[4 * e + h] = u[h] * rcp_approx(qp[h]);
-                }
+                const int bb = hf * 4 + 2 * t2 + e;          // block within the word
+                gen_pair<K>((word >> (4 * bb)) & 0xFu, qi, P + bb * 4 * K, U + 4 * e, W + 4 * e);
             }
-            const uint32_t off = (r >> 3) * SBO_STD + (hf * 4 + t2) * LBO_STD + (r & 7) * 16;
+            const uint32_t off = (r >> 3) * SBO_STD + (hf * 2 + t2) * LBO_STD + (r & 7) * 16;
             uint32_t wh[4], wl[4], uh[4], ul[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -260,50 +365,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_accum_q_tc(PassArgs a) {
         fence_async_smem();
         fence_before();
         __syncthreads();
-        const int win = s / TC_FLUSH;
-        const int d = win & 1;
-        if (tid == 0) {
-            fence_after();
-            issue_stage<K>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, bB, (s % TC_FLUSH) == 0);
-            commit(&sy->mma_done[b]);
-            if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
-            sy->issued = s + 1;
-        }
-        // fold the previous window while the tensor core runs this stage
-        if ((s % TC_FLUSH) == 0 && s > 0) {
-            const int wp = win - 1;
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
-            if (!ok) set_bad(sy, a.slots);
-            else {
-                fence_after();
-                flush_window<D::HALF>(tmem, lane_base, (wp & 1) * D::NT, col0, acc, comp);
-            }
-            fence_before();
-        }
+        issue_and_fold<K>(sy, a.slots, tid, hf, s, ns, b, tmem, taddr_lane, aB, A_TILE_STD, LBO_STD, SBO_STD, bB, acc,
+                          comp);
     }
-    // last window
-    __syncthreads();
-    if (ns > 0 && !sy->bad) {
-        const int wl = (ns - 1) / TC_FLUSH;
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wl & 1], (wl >> 1) & 1, TC_BUDGET));
-        if (!ok) set_bad(sy, a.slots);
-        else {
-            fence_after();
-            flush_window<D::HALF>(tmem, lane_base, (wl & 1) * D::NT, col0, acc, comp);
-        }
-    }
-    drain(sy, ns);
-    fence_before();
-    __syncthreads();
+    final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
     // write partials: v < K gradient, v = K + tri index Hessian
     constexpr int NV = K + D::NH;
     double* out = a.part + (int64_t)blockIdx.y * NV * a.Ipad;
 #pragma unroll
     for (int c = 0; c < D::HALF; ++c) {
-        const int col = col0 + c;
-        const double val = (double)acc[c] - (double)comp[c];
-        if (col < D::NH) out[(int64_t)(K + col) * a.Ipad + i] = val;
-        else if (col >= D::NHP && col < D::NHP + K) out[(int64_t)(col - D::NHP) * a.Ipad + i] = val * G_UNSCALE;
+        const int col = hf * D::HALF + c;
+        if (col < D::NH) {
+            out[(int64_t)(K + col) * a.Ipad + i] = (double)acc[c];
+        } else if (col >= D::NHP && col < D::NHP + K) {
+            out[(int64_t)(col - D::NHP) * a.Ipad + i] = (double)acc[c] * G_UNSCALE;
+        }
     }
     if (warp == 0) {
         fence_after();
@@ -312,174 +388,152 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_accum_q_tc(PassArgs a) {
 }
 
 // ------------------------------------------------------------------ P side
+// CTA: 32 blocks (128 haplotype columns = TMEM lanes) x a chunk of individuals;
+// stage = 32 individuals.  Thread (jl, ig): block jl, individuals 4ig..4ig+3.
 template <int K>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_accum_p_tc(PassArgs a) {
+__global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(PassArgs a) {
     using D = TcDims<K>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_PAD]
     const uint32_t sB = sA + 2 * 4 * A_TILE_PAD;                     // [2][2][B_TILE]
-    float* Q32 = (float*)(smem + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE);   // [2][64 * K]
-    uint32_t* SW = (uint32_t*)(Q32 + 2 * 64 * K);                    // [2][4][64]
-    Sync* sy = (Sync*)(SW + 2 * 4 * 64);
+    float* Q32 = (float*)(smem + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE);   // [2][KD * K]
+    uint32_t* SW = (uint32_t*)(Q32 + 2 * KD * K);                    // [2][4][KD]
+    Sync* sy = (Sync*)(SW + 2 * 4 * KD);
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int jl = tid >> 3, ig = tid & 7;
+    const int hf = tid >> 7;
     const int64_t j = (int64_t)blockIdx.x * 32 + jl;
     const bool valid = j < a.J;
     const int64_t i0 = (int64_t)blockIdx.y * a.per_chunk;
     const int64_t i1 = min(a.I, i0 + (int64_t)a.per_chunk);
-    const int ns = (int)((i1 - i0 + 63) / 64);
+    const int ns = (int)((i1 - i0 + KD - 1) / KD);
 
     if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
-    if (tid == 0) {
-        mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
-        mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
-        sy->bad = 0;
-        sy->issued = 0;
-        mbar_fence_init();
-    }
+    init_sync(sy, tid);
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = sy->tslot;
+    const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
 
-    float pr[4][K];
+    float pr[4 * K];
 #pragma unroll
-    for (int h = 0; h < 4; ++h)
+    for (int t = 0; t < 4 * K; ++t) pr[t] = valid ? (float)a.p[(int64_t)K * 4 * j + t] : 0.25f;
+    float acc[D::HALF], comp[D::NG];
 #pragma unroll
-        for (int k = 0; k < K; ++k) pr[h][k] = valid ? (float)a.p[(int64_t)K * (4 * j + h) + k] : 0.25f;
-    float acc[D::HALF], comp[D::HALF];
+    for (int c = 0; c < D::HALF; ++c) acc[c] = 0.f;
 #pragma unroll
-    for (int c = 0; c < D::HALF; ++c) { acc[c] = 0.f; comp[c] = 0.f; }
-    const int r = tid & 127, hf = tid >> 7;
-    const int lane_base = 32 * (warp & 3);
-    const int col0 = hf * D::HALF;
+    for (int c = 0; c < D::NG; ++c) comp[c] = 0.f;
     const int bsh = 4 * (jl & 7);
+
+    // staging roles: q values (VPT per thread) and class words (threads < 4*KD)
+    const int sw_w = tid / KD, sw_i = tid % KD;                      // word column, individual
+    const int64_t sw_jw = (int64_t)blockIdx.x * 4 + sw_w;
+    float qv_nx[D::VPT];
+    uint32_t w_nx = HX_PAD_WORD;
+    {
+        const int64_t n0 = min((int64_t)KD, i1 - i0);
+        if (tid < 4 * KD && sw_i < n0 && sw_jw < a.JW) w_nx = a.G[sw_jw * a.Ipad + i0 + sw_i];
+#pragma unroll
+        for (int v = 0; v < D::VPT; ++v) {
+            const int t = tid + v * TC_THREADS;
+            qv_nx[v] = (t < (int)n0 * K) ? (float)a.q[(int64_t)K * i0 + t] : 1.f / K;
+        }
+    }
 
     for (int s = 0; s < ns; ++s) {
         const int b = s & 1;
+        float* Qs = Q32 + b * KD * K;
+        uint32_t* Ws = SW + b * 4 * KD;
         if (s >= 2 && !sy->bad) {
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         }
-        const int64_t is = i0 + 64 * (int64_t)s;
-        const int n = (int)min((int64_t)64, i1 - is);
-        float* Qs = Q32 + b * 64 * K;
-        uint32_t* Ws = SW + b * 4 * 64;
-        for (int t = tid; t < 64 * K; t += TC_THREADS) Qs[t] = (t < n * K) ? (float)a.q[(int64_t)K * is + t] : 1.f / K;
-        {
-            const int w = tid >> 6, ii = tid & 63;
-            const int64_t jw = (int64_t)blockIdx.x * 4 + w;
-            Ws[tid] = (ii < n && jw < a.JW) ? a.G[jw * a.Ipad + is + ii] : HX_PAD_WORD;
+#pragma unroll
+        for (int v = 0; v < D::VPT; ++v) {
+            const int t = tid + v * TC_THREADS;
+            if (t < KD * K) Qs[t] = qv_nx[v];
+        }
+        if (tid < 4 * KD) Ws[tid] = w_nx;
+        if (s + 1 < ns) {
+            const int64_t isn = i0 + (int64_t)KD * (s + 1);
+            const int64_t nn = min((int64_t)KD, i1 - isn);
+            w_nx = (tid < 4 * KD && sw_i < nn && sw_jw < a.JW) ? a.G[sw_jw * a.Ipad + isn + sw_i] : HX_PAD_WORD;
+#pragma unroll
+            for (int v = 0; v < D::VPT; ++v) {
+                const int t = tid + v * TC_THREADS;
+                qv_nx[v] = (t < (int)nn * K) ? (float)a.q[(int64_t)K * isn + t] : 1.f / K;
+            }
         }
         __syncthreads();
         if (sy->bad) break;
         const uint32_t bB = sB + b * 2 * D::B_TILE;
-        for (int it = tid; it < D::NT * 8; it += TC_THREADS) {
+        for (int it = tid; it < D::NT * (KD / 8); it += TC_THREADS) {
             const int nn = it % D::NT, kg = it / D::NT;
             const uint32_t off = (nn >> 3) * SBO_STD + kg * LBO_STD + (nn & 7) * 16;
-            b_item<K>(Qs + kg * 8 * K, K, nn, bB + off, bB + D::B_TILE + off);
+            b_item<K>(Qs + kg * 8 * K, nn, bB + off, bB + D::B_TILE + off);
         }
-        // A = W^T tile: rows m = 4*jl + h, reduction over the stage's 64 individuals
-        float W[4][8], U[4][8];
+        // A = W^T tile: rows m = 4*jl + h, reduction over the stage's individuals
+        float W[4][4], U[4][4];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int ii = ig * 8 + e;
-            const unsigned nib = (Ws[(jl >> 3) * 64 + ii] >> bsh) & 0xFu;
-            const float* qr = Qs + ii * K;
+        for (int e = 0; e < 4; ++e) {
+            const int ii = ig * 4 + e;
+            const unsigned nib = (Ws[(jl >> 3) * KD + ii] >> bsh) & 0xFu;
             float qv[K];
 #pragma unroll
-            for (int k = 0; k < K; ++k) qv[k] = qr[k];
-            float qp[4];
+            for (int k = 0; k < K; ++k) qv[k] = Qs[ii * K + k];
+            float u4[4], w4[4];
+            gen_pair<K>(nib, qv, pr, u4, w4);
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                float sm = 0.f;
-#pragma unroll
-                for (int k = 0; k < K; ++k) sm = fmaf(qv[k], pr[h][k], sm);
-                qp[h] = sm;
-            }
-            float L, u[4];
-            pair_eval<float>(nib, qp, L, u);
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                U[h][e] = u[h] * U_SCALE;
-                W[h][e] = u[h] * rcp_approx(qp[h]);
-            }
+            for (int h = 0; h < 4; ++h) { U[h][e] = u4[h]; W[h][e] = w4[h]; }
         }
         const uint32_t aB = sA + b * 4 * A_TILE_PAD;
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
             const int m = 4 * jl + h;
-            const uint32_t off = (m >> 3) * SBO_PAD + ig * LBO_PAD + (m & 7) * 16;
-            uint32_t wh[4], wl[4], uh[4], ul[4];
+            const uint32_t off = (m >> 3) * SBO_PAD + (ig >> 1) * LBO_PAD + (m & 7) * 16 + (ig & 1) * 8;
+            uint32_t wh[2], wl[2], uh[2], ul[2];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
+            for (int e = 0; e < 2; ++e) {
                 split2(W[h][2 * e], W[h][2 * e + 1], wh[e], wl[e]);
                 split2_f16(U[h][2 * e], U[h][2 * e + 1], uh[e], ul[e]);
             }
-            sts128(aB + off, wh[0], wh[1], wh[2], wh[3]);
-            sts128(aB + A_TILE_PAD + off, wl[0], wl[1], wl[2], wl[3]);
-            sts128(aB + 2 * A_TILE_PAD + off, uh[0], uh[1], uh[2], uh[3]);
-            sts128(aB + 3 * A_TILE_PAD + off, ul[0], ul[1], ul[2], ul[3]);
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + off), "r"(wh[0]), "r"(wh[1]) : "memory");
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + A_TILE_PAD + off), "r"(wl[0]), "r"(wl[1]) : "memory");
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + 2 * A_TILE_PAD + off), "r"(uh[0]), "r"(uh[1]) : "memory");
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + 3 * A_TILE_PAD + off), "r"(ul[0]), "r"(ul[1]) : "memory");
         }
         fence_async_smem();
         fence_before();
         __syncthreads();
-        const int win = s / TC_FLUSH;
-        const int d = win & 1;
-        if (tid == 0) {
-            fence_after();
-            issue_stage<K>(tmem, d * D::NT, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, bB, (s % TC_FLUSH) == 0);
-            commit(&sy->mma_done[b]);
-            if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
-            sy->issued = s + 1;
-        }
-        if ((s % TC_FLUSH) == 0 && s > 0) {
-            const int wp = win - 1;
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
-            if (!ok) set_bad(sy, a.slots);
-            else {
-                fence_after();
-                flush_window<D::HALF>(tmem, lane_base, (wp & 1) * D::NT, col0, acc, comp);
-            }
-            fence_before();
-        }
+        issue_and_fold<K>(sy, a.slots, tid, hf, s, ns, b, tmem, taddr_lane, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, bB, acc,
+                          comp);
     }
-    __syncthreads();
-    if (ns > 0 && !sy->bad) {
-        const int wl = (ns - 1) / TC_FLUSH;
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wl & 1], (wl >> 1) & 1, TC_BUDGET));
-        if (!ok) set_bad(sy, a.slots);
-        else {
-            fence_after();
-            flush_window<D::HALF>(tmem, lane_base, (wl & 1) * D::NT, col0, acc, comp);
-        }
-    }
-    drain(sy, ns);
-    fence_before();
-    __syncthreads();
+    final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
     // rows m of this CTA: TMEM lane r
+    const int r = tid & 127;
     const int64_t m = (int64_t)blockIdx.x * 128 + r;
     if (m < 4 * a.J) {
         constexpr int NV = K + D::NH;
+        const int64_t rows = 4 * a.J;
 #pragma unroll
         for (int c = 0; c < D::HALF; ++c) {
-            const int col = col0 + c;
-            const double val = (double)acc[c] - (double)comp[c];
-            if (a.S == 1) {
-                if (col < D::NH) {
+            const int col = hf * D::HALF + c;
+            if (col < D::NH) {
+                const double val = (double)acc[c];
+                if (a.S == 1) {
                     int k, k2;
                     tri_pair<K>(col, k, k2);
                     a.XtX[(int64_t)K * K * m + k2 + K * k] = val;
                     a.XtX[(int64_t)K * K * m + k + K * k2] = val;
-                } else if (col >= D::NHP && col < D::NHP + K) {
-                    a.Xtz[(int64_t)K * m + (col - D::NHP)] = val * G_UNSCALE;
+                } else {
+                    a.part[((int64_t)blockIdx.y * NV + K + col) * rows + m] = val;
                 }
-            } else {
-                const int64_t rows = 4 * a.J;
-                double* out = a.part + (int64_t)blockIdx.y * NV * rows;
-                if (col < D::NH) out[(int64_t)(K + col) * rows + m] = val;
-                else if (col >= D::NHP && col < D::NHP + K) out[(int64_t)(col - D::NHP) * rows + m] = val * G_UNSCALE;
+            } else if (col >= D::NHP && col < D::NHP + K) {
+                const double val = (double)acc[c] * G_UNSCALE;
+                if (a.S == 1) a.Xtz[(int64_t)K * m + (col - D::NHP)] = val;
+                else a.part[((int64_t)blockIdx.y * NV + (col - D::NHP)) * rows + m] = val;
             }
         }
     }
@@ -491,11 +545,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_accum_p_tc(PassArgs a) {
 
 template <int K> constexpr size_t smem_q() {
     using D = TcDims<K>;
-    return 1024 + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE + 2 * 64 * K * 4 + sizeof(Sync);
+    return 1024 + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE + 2 * KD * K * 4 + sizeof(Sync);
 }
 template <int K> constexpr size_t smem_p() {
     using D = TcDims<K>;
-    return 1024 + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE + 2 * 64 * K * 4 + 2 * 4 * 64 * 4 + sizeof(Sync);
+    return 1024 + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE + 2 * KD * K * 4 + 2 * 4 * KD * 4 + sizeof(Sync);
 }
 
 #define HX_FOR_K(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
