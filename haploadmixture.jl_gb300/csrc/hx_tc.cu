@@ -68,7 +68,18 @@ struct Sync {
     uint32_t tslot;
     int bad;
     int issued;     // stages whose MMAs have been issued
+    uint32_t arrived[2];   // generator threads done with stage buffer b
 };
+
+// Arrival on the stage buffer: returns true for the last of the TC_THREADS
+// generator threads.  Release/acquire ordering (after each writer's
+// fence.proxy.async) makes every thread's tile stores visible to the MMAs
+// that the last arriver issues.
+__device__ __forceinline__ bool arrive_last(uint32_t* ctr, uint32_t total) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;" : "=r"(old) : "r"(smem_u32(ctr)) : "memory");
+    return old == total - 1;
+}
 
 __device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
     sy->bad = 1;
@@ -209,6 +220,8 @@ __device__ __forceinline__ void init_sync(Sync* sy, int tid) {
         mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
         sy->bad = 0;
         sy->issued = 0;
+        sy->arrived[0] = 0;
+        sy->arrived[1] = 0;
         mbar_fence_init();
     }
 }
@@ -222,7 +235,9 @@ __device__ __forceinline__ void issue_and_fold(Sync* sy, double* slots, int tid,
     using D = TcDims<K>;
     const int win = s / TC_FLUSH;
     const int d = win & 1;
-    if (tid == 0) {
+    (void)tid;
+    if (arrive_last(&sy->arrived[b], TC_THREADS)) {
+        sy->arrived[b] = 0;          // next touched at stage s+2, after two barriers
         fence_after();
         issue_stage<K>(tmem, d * D::NT, aB, aStride, aLBO, aSBO, bB, (s % TC_FLUSH) == 0);
         commit(&sy->mma_done[b]);
@@ -364,7 +379,6 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         }
         fence_async_smem();
         fence_before();
-        __syncthreads();
         issue_and_fold<K>(sy, a.slots, tid, hf, s, ns, b, tmem, taddr_lane, aB, A_TILE_STD, LBO_STD, SBO_STD, bB, acc,
                           comp);
     }
@@ -506,7 +520,6 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         }
         fence_async_smem();
         fence_before();
-        __syncthreads();
         issue_and_fold<K>(sy, a.slots, tid, hf, s, ns, b, tmem, taddr_lane, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, bB, acc,
                           comp);
     }

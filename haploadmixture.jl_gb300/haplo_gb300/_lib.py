@@ -76,6 +76,7 @@ SIGNATURES = {
     "hx_kernel_stats": (I32, [P, I32, C.POINTER(I64), D]),
     "hx_reset_stats": (I32, [P]),
     "hx_synth_bed_device": (I32, [C.c_uint64, I64, I64, I32, P, P, C.c_double, P, I32]),
+    "hx_loglikelihood_noalloc": (I32, [P, I64, I64, I64, I32, P, P, I32, P, P]),
 }
 
 _lib = None

@@ -176,6 +176,35 @@ int hx_reset_stats(hx_ctx* ctx);
 int hx_synth_bed_device(uint64_t seed, int64_t I, int64_t J, int32_t K, const uint64_t* thrQ,
                         const uint64_t* thrP, double miss, uint8_t* d_bed, int32_t device);
 
+/* ---- log-likelihood without device allocation ----
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory at call time: frameworks that hand out all device memory
+ * from their own pool (CUDA.jl, the PyTorch caching allocator) and forbid side
+ * allocations, or latency-critical loops where cudaMalloc/cudaFree would
+ * synchronise the device.  Evaluates the same log-likelihood as
+ * hx_loglikelihood (src/loops.jl:236-258) straight from caller-owned device
+ * buffers: d_bed (first I individuals x first 2J SNPs of the SNP-major BED
+ * matrix, bytes_per_snp bytes per SNP), d_q (K x I) and d_p (K x 4J), FP64,
+ * column-major; writes one double to d_ll.  Kernels are enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream); the call does not
+ * synchronise.
+ *
+ * Its only scratch is a file-scope device array of HX_NOALLOC_SCRATCH doubles
+ * (256 KB), held by every GPU that loads this library until the process exits.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress, with the device current); make that first call before
+ * any stream capture.  Every call shares the array and leaves its partial sums
+ * in it; each call overwrites all the partials it reads, so nothing needs to
+ * start at zero.  Calls that overlap on the GPU (different streams, or other
+ * host threads) race on the array and must be serialised by the caller.
+ * Returns HX_EUNSUPPORTED when ceil(I/128) exceeds HX_NOALLOC_SCRATCH
+ * (I > 4,194,304) or K is outside 1..HX_KMAX, HX_EINVAL for bad arguments, and
+ * HX_ECUDA on a CUDA error.  Calls no cudaMalloc, cudaFree or allocating
+ * library routine. */
+#define HX_NOALLOC_SCRATCH 32768
+int hx_loglikelihood_noalloc(const uint8_t* d_bed, int64_t bytes_per_snp, int64_t I, int64_t J, int32_t K,
+                             const double* d_q, const double* d_p, int32_t precision, double* d_ll, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
