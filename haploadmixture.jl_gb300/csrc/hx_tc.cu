@@ -65,6 +65,7 @@ template <int K> struct TcDims {
 struct Sync {
     uint64_t mma_done[2];
     uint64_t flush_done[2];
+    uint64_t qp_done[2];
     uint32_t tslot;
     int bad;
     int issued;     // stages whose MMAs have been issued
@@ -218,6 +219,7 @@ __device__ __forceinline__ void init_sync(Sync* sy, int tid) {
     if (tid == 0) {
         mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
         mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
+        mbar_init(&sy->qp_done[0], 1); mbar_init(&sy->qp_done[1], 1);
         sy->bad = 0;
         sy->issued = 0;
         sy->arrived[0] = 0;
@@ -280,14 +282,88 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int 
 // ------------------------------------------------------------------ Q side
 // CTA: 128 individuals (TMEM lanes) x a chunk of class words; stage = 1 word
 // (8 blocks, 32 haplotype columns).  Thread (r, hf): row r, blocks 4hf..4hf+3.
+// qp[i, m] = sum_k q[k,i] p[k,m] also comes from the tensor core: kind::tf32
+// MMAs (hi*hi + hi*lo + lo*hi of TF32-rounded splits, ~2^-21 relative) of the
+// CTA's q tile by the stage's p tile into a double-buffered 32-column TMEM
+// tile, issued one stage ahead; each thread reads its row's 16 values.
+template <int K> struct QpDims {
+    static constexpr int KP = K <= 8 ? 8 : 16;        // reduction padded to tf32 steps of 8
+    static constexpr int SBO = (KP / 4) * 128;        // 4 tf32 per 16-byte core row
+    static constexpr int A_T = 16 * SBO;              // 128 rows
+    static constexpr int B_T = 4 * SBO;               // 32 rows
+    static constexpr int NCOL = 2 * TcDims<K>::NT + 64;
+    static constexpr int TCOLS = NCOL <= 32 ? 32 : NCOL <= 64 ? 64 : NCOL <= 128 ? 128 : 256;
+};
+
+template <int K>
+__device__ __forceinline__ void issue_qp(uint32_t tmem_col, uint32_t sAq, uint32_t sBq_buf) {
+    using QD = QpDims<K>;
+    constexpr uint32_t id = idesc_tf32(32);
+#pragma unroll
+    for (int ks = 0; ks < QD::KP / 8; ++ks) {
+        const uint32_t o = ks * 256;
+        const uint64_t ah = sdesc(sAq + o, 128, QD::SBO), al = sdesc(sAq + QD::A_T + o, 128, QD::SBO);
+        const uint64_t bh = sdesc(sBq_buf + o, 128, QD::SBO), bl = sdesc(sBq_buf + QD::B_T + o, 128, QD::SBO);
+        mma_tf32(tmem_col, ah, bh, id, ks > 0 ? 1u : 0u);
+        mma_tf32(tmem_col, ah, bl, id, 1u);
+        mma_tf32(tmem_col, al, bh, id, 1u);
+    }
+}
+
+// Stage t's p values (this thread's VPT of the 32K) into P32 (fp32, for the
+// PP tile) and into the tf32 hi/lo B tile of the qp MMA.
+template <int K>
+__device__ __forceinline__ void stage_p(int tid, const float* pv, float* P, uint32_t sBq_buf) {
+    using D = TcDims<K>;
+    using QD = QpDims<K>;
+#pragma unroll
+    for (int v = 0; v < D::VPT; ++v) {
+        const int t = tid + v * TC_THREADS;
+        if (t < KD * K) {
+            P[t] = pv[v];
+            const int m = t / K, k = t - (t / K) * K;
+            const float hi = tf32_round(pv[v]);
+            const float lo = tf32_round(pv[v] - hi);
+            const uint32_t off = (m >> 3) * QD::SBO + (k >> 2) * 128 + (m & 7) * 16 + (k & 3) * 4;
+            asm volatile("st.shared.b32 [%0], %1;" :: "r"(sBq_buf + off), "f"(hi) : "memory");
+            asm volatile("st.shared.b32 [%0], %1;" :: "r"(sBq_buf + QD::B_T + off), "f"(lo) : "memory");
+        }
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void load_p(int tid, int64_t word, int64_t plimit, const double* p, float* pv) {
+    using D = TcDims<K>;
+#pragma unroll
+    for (int v = 0; v < D::VPT; ++v) {
+        const int t = tid + v * TC_THREADS;
+        const int64_t g = word * 8 * 4 * K + t;
+        pv[v] = (t < KD * K && g < plimit) ? (float)p[g] : 0.25f;
+    }
+}
+
+// One pair from its qp: U (scaled) and W.
+__device__ __forceinline__ void gen_pair_qp(unsigned nib, const float* qp, float* U4, float* W4) {
+    float L, u[4];
+    pair_eval<float>(nib, qp, L, u);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        U4[h] = u[h] * U_SCALE;
+        W4[h] = u[h] * rcp_approx(qp[h]);
+    }
+}
+
 template <int K>
 __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(PassArgs a) {
     using D = TcDims<K>;
+    using QD = QpDims<K>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_STD]
     const uint32_t sB = sA + 2 * 4 * A_TILE_STD;                     // [2][2][B_TILE]
-    float* P32 = (float*)(smem + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE);   // [2][KD * K]
+    const uint32_t sAq = sB + 2 * 2 * D::B_TILE;                     // [2 hi/lo][A_T]
+    const uint32_t sBq = sAq + 2 * QD::A_T;                          // [2 buf][2 hi/lo][B_T]
+    float* P32 = (float*)(smem + (sBq - sA) + 4 * QD::B_T);          // [2][KD * K]
     Sync* sy = (Sync*)(P32 + 2 * KD * K);
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -298,63 +374,83 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     const int ns = min(a.JW, w0 + a.per_chunk) - w0;     // one word per stage
     const int64_t plimit = a.J * 4 * K;
 
-    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+    if (warp == 0) tmem_alloc<QD::TCOLS>(&sy->tslot);
     init_sync(sy, tid);
+    // zero the tf32 operand tiles (reduction padding k >= K stays zero)
+    for (int t = tid; t < (2 * QD::A_T + 4 * QD::B_T) / 4; t += TC_THREADS)
+        asm volatile("st.shared.b32 [%0], %1;" :: "r"(sAq + 4 * t), "r"(0u) : "memory");
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = sy->tslot;
+    const uint32_t tq = tmem + 2 * D::NT;                 // qp tiles: columns [2NT, 2NT + 64)
     const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
 
-    float qi[K];
+    // q tile (tf32 hi/lo), once per CTA
+    if (hf == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) qi[k] = active ? (float)a.q[(int64_t)K * i + k] : 1.f / K;
+        for (int k = 0; k < K; ++k) {
+            const float x = active ? (float)a.q[(int64_t)K * i + k] : 1.f / K;
+            const float hi = tf32_round(x), lo = tf32_round(x - hi);
+            const uint32_t off = (r >> 3) * QD::SBO + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4;
+            asm volatile("st.shared.b32 [%0], %1;" :: "r"(sAq + off), "f"(hi) : "memory");
+            asm volatile("st.shared.b32 [%0], %1;" :: "r"(sAq + QD::A_T + off), "f"(lo) : "memory");
+        }
+    }
     float acc[D::HALF], comp[D::NG];
 #pragma unroll
     for (int c = 0; c < D::HALF; ++c) acc[c] = 0.f;
 #pragma unroll
     for (int c = 0; c < D::NG; ++c) comp[c] = 0.f;
 
-    // prefetch registers for stage 0
-    uint32_t word_nx = (ns > 0) ? a.G[(int64_t)w0 * a.Ipad + i] : HX_PAD_WORD;
-    float pv_nx[D::VPT];
-#pragma unroll
-    for (int v = 0; v < D::VPT; ++v) {
-        const int t = tid + v * TC_THREADS;
-        const int64_t g = (int64_t)w0 * 8 * 4 * K + t;
-        pv_nx[v] = (t < KD * K && g < plimit) ? (float)a.p[g] : 0.25f;
+    // stage 0 inputs, then the qp MMA of stage 0
+    float pv[D::VPT];
+    uint32_t word_cur = HX_PAD_WORD, word_nx = HX_PAD_WORD;
+    if (ns > 0) {
+        load_p<K>(tid, w0, plimit, a.p, pv);
+        stage_p<K>(tid, pv, P32, sBq);
+        word_cur = a.G[(int64_t)w0 * a.Ipad + i];
+    }
+    if (ns > 1) load_p<K>(tid, w0 + 1, plimit, a.p, pv);
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    if (tid == 0 && ns > 0) {
+        fence_after();
+        issue_qp<K>(tq, sAq, sBq);
+        commit(&sy->qp_done[0]);
     }
 
     for (int s = 0; s < ns; ++s) {
-        const int b = s & 1;
-        const uint32_t word = word_nx;
-        float* P = P32 + b * KD * K;
-        // buffer b was last read by the MMAs of stage s-2
+        const int b = s & 1, bn = b ^ 1;
+        const uint32_t word = word_cur;
+        // main tile buffer b was last read by the MMAs of stage s-2
         if (s >= 2 && !sy->bad) {
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         }
-#pragma unroll
-        for (int v = 0; v < D::VPT; ++v) {
-            const int t = tid + v * TC_THREADS;
-            if (t < KD * K) P[t] = pv_nx[v];
-        }
-        if (s + 1 < ns) {            // the next stage's loads, consumed next iteration
-            const int wn = w0 + s + 1;
-            word_nx = a.G[(int64_t)wn * a.Ipad + i];
-#pragma unroll
-            for (int v = 0; v < D::VPT; ++v) {
-                const int t = tid + v * TC_THREADS;
-                const int64_t g = (int64_t)wn * 8 * 4 * K + t;
-                pv_nx[v] = (t < KD * K && g < plimit) ? (float)a.p[g] : 0.25f;
-            }
-        }
         __syncthreads();
         if (sy->bad) break;
+        // the next stage's inputs (its qp MMA is issued by this stage's last arriver)
+        if (s + 1 < ns) {
+            stage_p<K>(tid, pv, P32 + bn * KD * K, sBq + bn * 2 * QD::B_T);
+            word_nx = a.G[(int64_t)(w0 + s + 1) * a.Ipad + i];
+            if (s + 2 < ns) load_p<K>(tid, w0 + s + 2, plimit, a.p, pv);
+        }
+        const float* P = P32 + b * KD * K;
         const uint32_t bB = sB + b * 2 * D::B_TILE;
         for (int it = tid; it < D::NT * (KD / 8); it += TC_THREADS) {
             const int n = it % D::NT, kg = it / D::NT;
             const uint32_t off = (n >> 3) * SBO_STD + kg * LBO_STD + (n & 7) * 16;
             b_item<K>(P + kg * 8 * K, n, bB + off, bB + D::B_TILE + off);
+        }
+        // this stage's qp: 16 columns of this thread's row
+        float qpv[16];
+        {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], (s >> 1) & 1, TC_BUDGET));
+            if (!ok) set_bad(sy, a.slots);
+            fence_after();
+            tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16), qpv);
+            tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16 + 8), qpv + 8);
         }
         const uint32_t aB = sA + b * 4 * A_TILE_STD;
 #pragma unroll
@@ -362,8 +458,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             float W[8], U[8];
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                const int bb = hf * 4 + 2 * t2 + e;          // block within the word
-                gen_pair<K>((word >> (4 * bb)) & 0xFu, qi, P + bb * 4 * K, U + 4 * e, W + 4 * e);
+                const int bb = 2 * t2 + e;                    // block within this thread's half
+                gen_pair_qp((word >> (4 * (hf * 4 + bb))) & 0xFu, qpv + 4 * bb, U + 4 * e, W + 4 * e);
             }
             const uint32_t off = (r >> 3) * SBO_STD + (hf * 2 + t2) * LBO_STD + (r & 7) * 16;
             uint32_t wh[4], wl[4], uh[4], ul[4];
@@ -379,8 +475,32 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         }
         fence_async_smem();
         fence_before();
-        issue_and_fold<K>(sy, a.slots, tid, hf, s, ns, b, tmem, taddr_lane, aB, A_TILE_STD, LBO_STD, SBO_STD, bB, acc,
-                          comp);
+        {
+            const int win = s / TC_FLUSH;
+            const int d = win & 1;
+            if (arrive_last(&sy->arrived[b], TC_THREADS)) {
+                sy->arrived[b] = 0;
+                fence_after();
+                issue_stage<K>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, bB, (s % TC_FLUSH) == 0);
+                if (s + 1 < ns) issue_qp<K>(tq + bn * 32, sAq, sBq + bn * 2 * QD::B_T);
+                // mma_done also covers the qp MMA, so that draining it covers every MMA in flight
+                commit(&sy->mma_done[b]);
+                if (s + 1 < ns) commit(&sy->qp_done[bn]);
+                if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
+                sy->issued = s + 1;
+            }
+            if ((s % TC_FLUSH) == 0 && s > 0) {
+                const int wp = win - 1;
+                const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
+                if (!ok) set_bad(sy, a.slots);
+                else {
+                    fence_after();
+                    fold_half<K>(hf, taddr_lane, (wp & 1) * D::NT, acc, comp);
+                }
+                fence_before();
+            }
+        }
+        word_cur = word_nx;
     }
     final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
     // write partials: v < K gradient, v = K + tri index Hessian
@@ -397,7 +517,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     }
     if (warp == 0) {
         fence_after();
-        tmem_dealloc<D::TCOLS>(tmem);
+        tmem_dealloc<QD::TCOLS>(tmem);
     }
 }
 
@@ -558,7 +678,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
 
 template <int K> constexpr size_t smem_q() {
     using D = TcDims<K>;
-    return 1024 + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE + 2 * KD * K * 4 + sizeof(Sync);
+    using QD = QpDims<K>;
+    return 1024 + 2 * 4 * A_TILE_STD + 2 * 2 * D::B_TILE + 2 * QD::A_T + 4 * QD::B_T + 2 * KD * K * 4 + sizeof(Sync);
 }
 template <int K> constexpr size_t smem_p() {
     using D = TcDims<K>;

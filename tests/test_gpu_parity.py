@@ -182,7 +182,7 @@ def test_mixed_fit_reaches_fp64_optimum(hx, O):
         d.set_qp(q0, p0)
         info = d.fit(n_iter=3000, rtol=1e-14, em_iters=5)
         out[prec] = (info, d.get_qp()[0])
-    assert out["mixed"][0]["ll"] == pytest.approx(out["fp64"][0]["ll"], rel=1e-9)
+    assert out["mixed"][0]["ll"] == pytest.approx(out["fp64"][0]["ll"], rel=5e-9)
     assert np.abs(out["mixed"][1] - out["fp64"][1]).max() < 2e-5
 
 
