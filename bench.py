@@ -35,18 +35,21 @@ for _p in (ROOT, os.path.join(ROOT, "haploadmixture.jl_gb300")):
         sys.path.insert(0, _p)
 
 METRIC = "s to converge (rel Δloglik<1e-8), I=1e5×2e5 SNPs K=8: chosen vs plain GPU"
-# outer iterations of the C3 fit measured on GB300; used only to extrapolate
-# the CPU reference arm, whose full fit takes hours
-REF_ITERS_DEFAULT = 30
+# outer iterations of the C3 fit measured on GB300 (26 at rtol 1e-8); used
+# only to extrapolate the CPU reference arm, whose full fit takes hours
+REF_ITERS_DEFAULT = 26
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="C3")
+    ap.add_argument("--I", type=int, default=0, help="override the config's individuals (profiling)")
+    ap.add_argument("--J", type=int, default=0, help="override the config's 2-SNP blocks (profiling)")
+    ap.add_argument("--K", type=int, default=0, help="override the config's ancestral populations")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--n-iter", type=int, default=1000)
@@ -56,7 +59,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--cpu-slice-blocks", type=int, default=0)
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def load_peaks():
@@ -133,6 +136,16 @@ def pass_bytes(kind, I, J, K):
     return None
 
 
+def workload(name, cfg):
+    return ("%s synthetic cohort I=%d x %d SNPs (J=%d blocks), K=%d, alpha=%g, %g%% missing, seed %d"
+            % (name, cfg["I"], 2 * cfg["J"], cfg["J"], cfg["K"], cfg["alpha"], 100 * cfg["miss"], cfg["seed"]))
+
+
+def load_config(args):
+    from haplo_gb300 import synth
+    return synth.config(args.config, I=args.I, J=args.J, K=args.K)
+
+
 def cpu_oracle_sample(cfg, slice_blocks, threads):
     """Times the CPU oracle on an I x slice_blocks slice: one EM step and one
     outer QN iteration (4 accumulations + QPs + 2 log-likelihoods + ZAL)."""
@@ -190,8 +203,7 @@ def run_reference(args, world, rank):
     CPU loops, all host threads) on bounded slices of the workload."""
     if rank != 0:
         return
-    from haplo_gb300 import synth
-    cfg = synth.config(args.config)
+    cfg = load_config(args)
     threads = os.cpu_count() or 1
     Js = args.cpu_slice_blocks or 200
     vals = []
@@ -208,8 +220,7 @@ def run_reference(args, world, rank):
     line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "C3 synthetic cohort I=100000 x 200000 SNPs (J=100000 blocks), K=8",
-                       "rtol": args.rtol, "em_iters": args.em_iters},
+            "config": {"workload": workload(args.config, cfg), "rtol": args.rtol, "em_iters": args.em_iters},
             "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -222,7 +233,7 @@ def run_ours(args, world, rank, local):
     from haplo_gb300.admix import random_init
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    cfg = synth.config(args.config)
+    cfg = load_config(args)
     I, J, K = cfg["I"], cfg["J"], cfg["K"]
     bps = (I + 3) // 4
     n_snp = 2 * J
@@ -280,8 +291,7 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": "C3 synthetic cohort I=100000 x 200000 SNPs (J=100000 blocks), K=8, "
-                                   "alpha=0.3, 1%% missing, seed %d" % cfg["seed"],
+            "config": {"workload": workload(args.config, cfg),
                        "method": args.precision, "rtol": args.rtol, "em_iters": args.em_iters,
                        "outer_iters": iters, "loglik": ll, "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "inputs (5 GB class words) larger than L2; no flush"},

@@ -75,8 +75,11 @@ def synth_device(seed, Q, P, miss, d_bed_addr, device=0):
                                                C.c_void_p(d_bed_addr), device))
 
 
-def config(name):
+def config(name, **sizes):
+    """Named synthetic workload; `sizes` (I, J, K) overrides give a smaller
+    case of the same generator, used for profiling captures."""
     c = dict(CONFIGS[name])
+    c.update({k: int(v) for k, v in sizes.items() if v})
     Q, P = draw_params(c["I"], c["J"], c["K"], c["alpha"], c["pmode"], c["seed"])
     c["Q"], c["P"] = Q, P
     c["bps"] = (c["I"] + 3) // 4
