@@ -93,6 +93,95 @@ __device__ __forceinline__ void pair_eval(unsigned nib, const T qp[4], T& L, T u
     }
 }
 
+// Copy-level allele indicators of a raw SNP code, as FP32 0/1 values
+// {copy 1 may carry allele 0, copy 1 allele 1, copy 2 allele 0, copy 2 allele 1}:
+// hom A1 (code 0) {0}{0}; missing (1) {0,1}{0,1}; het (2) {0}{1}; hom A2 (3) {1}{1}.
+// With M[a][b] = qp_{2a+b}, F_s = sum_{a in A_s, b in B_s} M[a][b] over the
+// copy-s sets of the block's two SNPs, which is the class_m1/class_m2 factor
+// for every class except the double heterozygote and double missing.
+// A kernel keeps the table in shared memory (snp_table_init by its first 16
+// threads, then a barrier) and reads one 16-byte row per SNP: the four rows
+// occupy distinct banks, so a warp's lookups never conflict.
+__device__ __forceinline__ void snp_table_init(float4* tab, int tid) {
+    if (tid < 16) {
+        const int c = tid >> 2, e = tid & 3;
+        const int bits = c == 0 ? 0x5 : c == 1 ? 0xF : c == 2 ? 0x9 : 0xA;   // bit e: indicator e
+        reinterpret_cast<float*>(tab)[tid] = (bits >> e) & 1 ? 1.f : 0.f;
+    }
+}
+
+// FP32 pair evaluation for the mixed method: same results as pair_eval<float>
+// (L identical; u to the last bit of an approximate reciprocal), with the class
+// turned into arithmetic on indicator rows instead of per-haplotype selects.
+__device__ __forceinline__ void pair_eval_tab(unsigned nib, const float qp[4], float& L, float u[4], const float4* tab) {
+    const float4 ta = tab[nib & 3u], tb = tab[(nib >> 2) & 3u];
+    const float v10 = fmaf(tb.y, qp[1], tb.x * qp[0]), v11 = fmaf(tb.y, qp[3], tb.x * qp[2]);
+    const float v20 = fmaf(tb.w, qp[1], tb.z * qp[0]), v21 = fmaf(tb.w, qp[3], tb.z * qp[2]);
+    float F1 = fmaf(ta.y, v11, ta.x * v10);
+    float F2 = fmaf(ta.w, v21, ta.z * v20);
+    const bool hh = nib == NIB_HH;
+    const bool mm = nib == NIB_MM;
+    const float den = fmaf(qp[1], qp[2], qp[0] * qp[3]);
+    F1 = hh ? den : F1;
+    F1 = mm ? 1.f : F1;
+    F2 = (hh || mm) ? 1.f : F2;
+    L = F1 * F2;
+    float r1, r2;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(F1));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r2) : "f"(F2));
+    const float hr = hh ? r1 : 0.f;
+    r1 = (hh || mm) ? 0.f : r1;
+    r2 = (hh || mm) ? 0.f : r2;
+    const float x10 = ta.x * r1, x11 = ta.y * r1, x20 = ta.z * r2, x21 = ta.w * r2;
+    u[0] = fmaf(hr, qp[3], fmaf(x10, tb.x, x20 * tb.z));
+    u[1] = fmaf(hr, qp[2], fmaf(x10, tb.y, x20 * tb.w));
+    u[2] = fmaf(hr, qp[1], fmaf(x11, tb.x, x21 * tb.z));
+    u[3] = fmaf(hr, qp[0], fmaf(x11, tb.y, x21 * tb.w));
+}
+
+// Likelihood only (log-likelihood passes).
+__device__ __forceinline__ float pair_lik_tab(unsigned nib, const float qp[4], const float4* tab) {
+    const float4 ta = tab[nib & 3u], tb = tab[(nib >> 2) & 3u];
+    const float v10 = fmaf(tb.y, qp[1], tb.x * qp[0]), v11 = fmaf(tb.y, qp[3], tb.x * qp[2]);
+    const float v20 = fmaf(tb.w, qp[1], tb.z * qp[0]), v21 = fmaf(tb.w, qp[3], tb.z * qp[2]);
+    float F1 = fmaf(ta.y, v11, ta.x * v10);
+    float F2 = fmaf(ta.w, v21, ta.z * v20);
+    const bool hh = nib == NIB_HH;
+    const bool mm = nib == NIB_MM;
+    const float den = fmaf(qp[1], qp[2], qp[0] * qp[3]);
+    F1 = hh ? den : F1;
+    F1 = mm ? 1.f : F1;
+    F2 = (hh || mm) ? 1.f : F2;
+    return F1 * F2;
+}
+
+// Type-generic entry: FP32 uses the indicator table, FP64 the exact select form.
+__device__ __forceinline__ void pair_eval_t(unsigned nib, const float qp[4], float& L, float u[4], const float4* tab) {
+    pair_eval_tab(nib, qp, L, u, tab);
+}
+__device__ __forceinline__ void pair_eval_t(unsigned nib, const double qp[4], double& L, double u[4], const float4*) {
+    pair_eval<double>(nib, qp, L, u);
+}
+
+__device__ __forceinline__ float pair_lik_t(unsigned nib, const float qp[4], const float4* tab) {
+    return pair_lik_tab(nib, qp, tab);
+}
+__device__ __forceinline__ double pair_lik_t(unsigned nib, const double qp[4], const float4*) {
+    const unsigned m1 = (unsigned)(TAB_M1 >> (4 * nib)) & 0xFu;
+    const unsigned m2 = (unsigned)(TAB_M2 >> (4 * nib)) & 0xFu;
+    double F1 = ((((m1 & 1u) ? qp[0] : 0.0) + ((m1 & 2u) ? qp[1] : 0.0)) + ((m1 & 4u) ? qp[2] : 0.0)) +
+                ((m1 & 8u) ? qp[3] : 0.0);
+    double F2 = ((((m2 & 1u) ? qp[0] : 0.0) + ((m2 & 2u) ? qp[1] : 0.0)) + ((m2 & 4u) ? qp[2] : 0.0)) +
+                ((m2 & 8u) ? qp[3] : 0.0);
+    const bool hh = nib == NIB_HH;
+    const bool mm = nib == NIB_MM;
+    const double den = qp[0] * qp[3] + qp[1] * qp[2];
+    F1 = hh ? den : F1;
+    F1 = mm ? 1.0 : F1;
+    F2 = (hh || mm) ? 1.0 : F2;
+    return F1 * F2;
+}
+
 // Exact exponent/mantissa split used to accumulate products of likelihoods
 // without underflow (one log per thread instead of two per pair).
 __device__ __forceinline__ float renorm(float m, int& e) {

@@ -59,7 +59,9 @@ k_accum_q(PassArgs a) {
     constexpr int NH = K * (K + 1) / 2;
     constexpr int NV = K + (HESS ? NH : 0);
     __shared__ T sp[QSTAGE_WORDS * 8 * 4 * K];
+    __shared__ float4 s_snp[4];
     const int tid = threadIdx.x;
+    snp_table_init(s_snp, tid);
     const int64_t i = (int64_t)blockIdx.x * ACC_THREADS + tid;
     const int w0 = blockIdx.y * a.per_chunk;
     const int w1 = min(a.JW, w0 + a.per_chunk);
@@ -105,7 +107,7 @@ k_accum_q(PassArgs a) {
                         qp[h] = s;
                     }
                     T L, u[4];
-                    pair_eval<T>(nib, qp, L, u);
+                    pair_eval_t(nib, qp, L, u, s_snp);
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
                         T g = gin[k];
@@ -157,7 +159,9 @@ k_accum_p(PassArgs a) {
     constexpr int NV = K + (HESS ? NH : 0);
     __shared__ T sq[PSTAGE_IND * K];
     __shared__ uint32_t sg[4 * PSTAGE_IND];
+    __shared__ float4 s_snp[4];
     const int tid = threadIdx.x;
+    snp_table_init(s_snp, tid);
     const int lane = tid & 31, warp = tid >> 5;
     const int b = tid >> 2, h = tid & 3;
     const int64_t j = (int64_t)blockIdx.x * 32 + b;
@@ -198,7 +202,7 @@ k_accum_p(PassArgs a) {
 #pragma unroll
             for (int t = 0; t < 4; ++t) qp[t] = __shfl_sync(0xffffffffu, own, (lane & ~3) | t);
             T L, u[4];
-            pair_eval<T>(nib, qp, L, u);
+            pair_eval_t(nib, qp, L, u, s_snp);
             const T uh = h == 0 ? u[0] : (h == 1 ? u[1] : (h == 2 ? u[2] : u[3]));
 #pragma unroll
             for (int k = 0; k < K; ++k) gin[k] = fma(uh, qr[k], gin[k]);
@@ -246,7 +250,9 @@ __global__ void __launch_bounds__(ACC_THREADS)
 k_loglik(PassArgs a) {
     __shared__ T sp[QSTAGE_WORDS * 8 * 4 * K];
     __shared__ double red[ACC_THREADS];
+    __shared__ float4 s_snp[4];
     const int tid = threadIdx.x;
+    snp_table_init(s_snp, tid);
     const int64_t i = (int64_t)blockIdx.x * ACC_THREADS + tid;
     const int w0 = blockIdx.y * a.per_chunk;
     const int w1 = min(a.JW, w0 + a.per_chunk);
@@ -286,17 +292,7 @@ k_loglik(PassArgs a) {
                         for (int k = 0; k < K; ++k) s = fma(qi[k], pb[hh * K + k], s);
                         qp[hh] = s;
                     }
-                    const unsigned m1 = (unsigned)(TAB_M1 >> (4 * nib)) & 0xFu;
-                    const unsigned m2 = (unsigned)(TAB_M2 >> (4 * nib)) & 0xFu;
-                    T F1 = ((((m1 & 1u) ? qp[0] : T(0)) + ((m1 & 2u) ? qp[1] : T(0))) + ((m1 & 4u) ? qp[2] : T(0))) +
-                           ((m1 & 8u) ? qp[3] : T(0));
-                    T F2 = ((((m2 & 1u) ? qp[0] : T(0)) + ((m2 & 2u) ? qp[1] : T(0))) + ((m2 & 4u) ? qp[2] : T(0))) +
-                           ((m2 & 8u) ? qp[3] : T(0));
-                    const bool hhc = nib == NIB_HH;
-                    const T den = qp[0] * qp[3] + qp[1] * qp[2];
-                    F1 = hhc ? den : F1;
-                    F2 = hhc ? T(1) : F2;
-                    T L = F1 * F2;
+                    T L = pair_lik_t(nib, qp, s_snp);
                     if (!(L > T(0))) {
                         if (L == T(0)) zero = true; else bad = true;
                         L = T(1);

@@ -166,7 +166,7 @@ __device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aB
 
 // B tile item: row n (PP column for n < NHP, P/Q column for n >= NHP), 8
 // consecutive reduction indices whose K-vectors start at vec0[e * K].
-template <int K>
+template <int K, int VS>
 __device__ __forceinline__ void b_item(const float* vec0, int n, uint32_t dst_hi, uint32_t dst_lo) {
     using D = TcDims<K>;
     float v[8];
@@ -174,7 +174,7 @@ __device__ __forceinline__ void b_item(const float* vec0, int n, uint32_t dst_hi
     if (n >= D::NHP) {
         const int kk = n - D::NHP;
 #pragma unroll
-        for (int e = 0; e < 8; ++e) v[e] = kk < K ? vec0[e * K + kk] * GB_SCALE : 0.f;
+        for (int e = 0; e < 8; ++e) v[e] = kk < K ? vec0[e * VS + kk] * GB_SCALE : 0.f;
 #pragma unroll
         for (int e = 0; e < 4; ++e) split2_f16(v[2 * e], v[2 * e + 1], h[e], l[e]);
     } else {
@@ -182,7 +182,7 @@ __device__ __forceinline__ void b_item(const float* vec0, int n, uint32_t dst_hi
             int k, k2;
             tri_pair<K>(n, k, k2);
 #pragma unroll
-            for (int e = 0; e < 8; ++e) v[e] = vec0[e * K + k] * vec0[e * K + k2];
+            for (int e = 0; e < 8; ++e) v[e] = vec0[e * VS + k] * vec0[e * VS + k2];
         } else {
 #pragma unroll
             for (int e = 0; e < 8; ++e) v[e] = 0.f;
@@ -197,7 +197,8 @@ __device__ __forceinline__ void b_item(const float* vec0, int n, uint32_t dst_hi
 // One (individual, block) pair: qp from q and p (4K values), then U (scaled)
 // and W.
 template <int K>
-__device__ __forceinline__ void gen_pair(unsigned nib, const float* qv, const float* pb, float* U4, float* W4) {
+__device__ __forceinline__ void gen_pair(unsigned nib, const float* qv, const float* pb, float* U4, float* W4,
+                                         const float4* tab) {
     float qp[4];
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
@@ -207,7 +208,7 @@ __device__ __forceinline__ void gen_pair(unsigned nib, const float* qv, const fl
         qp[h] = sm;
     }
     float L, u[4];
-    pair_eval<float>(nib, qp, L, u);
+    pair_eval_tab(nib, qp, L, u, tab);
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         U4[h] = u[h] * U_SCALE;
@@ -343,9 +344,9 @@ __device__ __forceinline__ void load_p(int tid, int64_t word, int64_t plimit, co
 }
 
 // One pair from its qp: U (scaled) and W.
-__device__ __forceinline__ void gen_pair_qp(unsigned nib, const float* qp, float* U4, float* W4) {
+__device__ __forceinline__ void gen_pair_qp(unsigned nib, const float* qp, float* U4, float* W4, const float4* tab) {
     float L, u[4];
-    pair_eval<float>(nib, qp, L, u);
+    pair_eval_tab(nib, qp, L, u, tab);
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         U4[h] = u[h] * U_SCALE;
@@ -365,9 +366,11 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     const uint32_t sBq = sAq + 2 * QD::A_T;                          // [2 buf][2 hi/lo][B_T]
     float* P32 = (float*)(smem + (sBq - sA) + 4 * QD::B_T);          // [2][KD * K]
     Sync* sy = (Sync*)(P32 + 2 * KD * K);
+    __shared__ float4 s_snp[4];
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int r = tid & 127, hf = tid >> 7;
+    snp_table_init(s_snp, tid);
     const int64_t i = (int64_t)blockIdx.x * 128 + r;
     const bool active = i < a.I;
     const int w0 = blockIdx.y * a.per_chunk;
@@ -441,7 +444,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         for (int it = tid; it < D::NT * (KD / 8); it += TC_THREADS) {
             const int n = it % D::NT, kg = it / D::NT;
             const uint32_t off = (n >> 3) * SBO_STD + kg * LBO_STD + (n & 7) * 16;
-            b_item<K>(P + kg * 8 * K, n, bB + off, bB + D::B_TILE + off);
+            b_item<K, K>(P + kg * 8 * K, n, bB + off, bB + D::B_TILE + off);
         }
         // this stage's qp: 16 columns of this thread's row
         float qpv[16];
@@ -459,7 +462,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int bb = 2 * t2 + e;                    // block within this thread's half
-                gen_pair_qp((word >> (4 * (hf * 4 + bb))) & 0xFu, qpv + 4 * bb, U + 4 * e, W + 4 * e);
+                gen_pair_qp((word >> (4 * (hf * 4 + bb))) & 0xFu, qpv + 4 * bb, U + 4 * e, W + 4 * e, s_snp);
             }
             const uint32_t off = (r >> 3) * SBO_STD + (hf * 2 + t2) * LBO_STD + (r & 7) * 16;
             uint32_t wh[4], wl[4], uh[4], ul[4];
@@ -524,6 +527,10 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
 // ------------------------------------------------------------------ P side
 // CTA: 32 blocks (128 haplotype columns = TMEM lanes) x a chunk of individuals;
 // stage = 32 individuals.  Thread (jl, ig): block jl, individuals 4ig..4ig+3.
+// Staged q rows have stride QSTR floats (an odd number of 16-byte units), so
+// the 8 individual groups of a warp read 8 distinct bank quads.
+template <int K> constexpr int qstr() { return K <= 4 ? 4 : 12; }
+
 template <int K>
 __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(PassArgs a) {
     using D = TcDims<K>;
@@ -531,11 +538,14 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_PAD]
     const uint32_t sB = sA + 2 * 4 * A_TILE_PAD;                     // [2][2][B_TILE]
-    float* Q32 = (float*)(smem + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE);   // [2][KD * K]
-    uint32_t* SW = (uint32_t*)(Q32 + 2 * KD * K);                    // [2][4][KD]
+    constexpr int QSTR = qstr<K>();
+    float* Q32 = (float*)(smem + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE);   // [2][KD * QSTR]
+    uint32_t* SW = (uint32_t*)(Q32 + 2 * KD * QSTR);                 // [2][4][KD]
     Sync* sy = (Sync*)(SW + 2 * 4 * KD);
+    __shared__ float4 s_snp[4];
 
     const int tid = threadIdx.x, warp = tid >> 5;
+    snp_table_init(s_snp, tid);
     const int jl = tid >> 3, ig = tid & 7;
     const int hf = tid >> 7;
     const int64_t j = (int64_t)blockIdx.x * 32 + jl;
@@ -579,7 +589,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
 
     for (int s = 0; s < ns; ++s) {
         const int b = s & 1;
-        float* Qs = Q32 + b * KD * K;
+        float* Qs = Q32 + b * KD * QSTR;
         uint32_t* Ws = SW + b * 4 * KD;
         if (s >= 2 && !sy->bad) {
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
@@ -587,7 +597,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
 #pragma unroll
         for (int v = 0; v < D::VPT; ++v) {
             const int t = tid + v * TC_THREADS;
-            if (t < KD * K) Qs[t] = qv_nx[v];
+            if (t < KD * K) Qs[(t / K) * QSTR + t % K] = qv_nx[v];
         }
         if (tid < 4 * KD) Ws[tid] = w_nx;
         if (s + 1 < ns) {
@@ -606,7 +616,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         for (int it = tid; it < D::NT * (KD / 8); it += TC_THREADS) {
             const int nn = it % D::NT, kg = it / D::NT;
             const uint32_t off = (nn >> 3) * SBO_STD + kg * LBO_STD + (nn & 7) * 16;
-            b_item<K>(Qs + kg * 8 * K, nn, bB + off, bB + D::B_TILE + off);
+            b_item<K, QSTR>(Qs + kg * 8 * QSTR, nn, bB + off, bB + D::B_TILE + off);
         }
         // A = W^T tile: rows m = 4*jl + h, reduction over the stage's individuals
         float W[4][4], U[4][4];
@@ -614,11 +624,15 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         for (int e = 0; e < 4; ++e) {
             const int ii = ig * 4 + e;
             const unsigned nib = (Ws[(jl >> 3) * KD + ii] >> bsh) & 0xFu;
-            float qv[K];
+            float qv[(K + 3) / 4 * 4];
+            const float4* q4 = reinterpret_cast<const float4*>(Qs + ii * QSTR);
 #pragma unroll
-            for (int k = 0; k < K; ++k) qv[k] = Qs[ii * K + k];
+            for (int c = 0; c < (K + 3) / 4; ++c) {
+                const float4 x = q4[c];
+                qv[4 * c] = x.x; qv[4 * c + 1] = x.y; qv[4 * c + 2] = x.z; qv[4 * c + 3] = x.w;
+            }
             float u4[4], w4[4];
-            gen_pair<K>(nib, qv, pr, u4, w4);
+            gen_pair<K>(nib, qv, pr, u4, w4, s_snp);
 #pragma unroll
             for (int h = 0; h < 4; ++h) { U[h][e] = u4[h]; W[h][e] = w4[h]; }
         }
@@ -683,7 +697,7 @@ template <int K> constexpr size_t smem_q() {
 }
 template <int K> constexpr size_t smem_p() {
     using D = TcDims<K>;
-    return 1024 + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE + 2 * KD * K * 4 + 2 * 4 * KD * 4 + sizeof(Sync);
+    return 1024 + 2 * 4 * A_TILE_PAD + 2 * 2 * D::B_TILE + 2 * KD * qstr<K>() * 4 + 2 * 4 * KD * 4 + sizeof(Sync);
 }
 
 #define HX_FOR_K(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
