@@ -35,6 +35,7 @@ struct hx_ctx {
     double *part_q = nullptr, *part_p = nullptr, *part_ll = nullptr, *part_qn = nullptr, *coef = nullptr;
     double* slots = nullptr;
     double* h_slots = nullptr;   // pinned
+    uint8_t* img = nullptr;      // B-operand image of the tensor-core passes
     int S_q = 1, wpc_q = 1, S_p = 1, ipc_p = 1;
     bool tc = false;                         // Hessian passes on the tensor cores
     int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
@@ -151,6 +152,7 @@ PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
     a.q = q; a.p = p; a.S = 1; a.per_chunk = 1;
     a.part = nullptr; a.XtX = nullptr; a.Xtz = nullptr;
     a.slots = c->slots;
+    a.img = c->img;
     return a;
 }
 
@@ -158,7 +160,7 @@ int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
     PassArgs a = pass_args(c, q, p);
     if (hess && c->tc) {
         a.S = c->S_qt; a.per_chunk = c->wpc_qt; a.part = c->part_q;
-        HX_LAUNCH(HX_KIND_ACCUM_Q, 1, launch_accum_q_tc(c->K, a, c->st));
+        HX_LAUNCH(HX_KIND_ACCUM_Q, 2, launch_accum_q_tc(c->K, a, c->st));
         HX_LAUNCH(HX_KIND_OTHER, 1, launch_reduce_sym(c->part_q, c->S_qt, c->K, true, c->I, c->Ipad, XtX, Xtz, c->st));
         return HX_OK;
     }
@@ -174,7 +176,7 @@ int pass_p(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
     PassArgs a = pass_args(c, q, p);
     if (hess && c->tc) {
         a.S = c->S_pt; a.per_chunk = c->ipc_pt; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;
-        HX_LAUNCH(HX_KIND_ACCUM_P, 1, launch_accum_p_tc(c->K, a, c->st));
+        HX_LAUNCH(HX_KIND_ACCUM_P, 2, launch_accum_p_tc(c->K, a, c->st));
         if (c->S_pt > 1)
             HX_LAUNCH(HX_KIND_OTHER, 1,
                       launch_reduce_sym(c->part_p, c->S_pt, c->K, true, 4 * c->J, 4 * c->J, XtX, Xtz, c->st));
@@ -323,6 +325,7 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (2 * HX_QMAX * HX_QMAX + HX_QMAX)));
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));
+    if (c->tc) HX_ST(dalloc(c, &c->img, tc_image_bytes(K, I, J)));
     HX_CK(cudaMallocHost((void**)&c->h_slots, HX_NSLOT * sizeof(double)));
     HX_CK(cudaMemsetAsync(c->U, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
     HX_CK(cudaMemsetAsync(c->V, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
@@ -423,7 +426,7 @@ int hx_destroy(hx_ctx* c) {
     if (!c) return HX_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     void* bufs[] = {c->G, c->dm, c->x, c->xn, c->xn2, c->xt, c->xio, c->U, c->V, c->XtXq, c->Xtzq, c->XtXp,
-                    c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots};
+                    c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots, c->img};
     for (void* b : bufs) if (b) cudaFree(b);
     prof_resolve(c);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);

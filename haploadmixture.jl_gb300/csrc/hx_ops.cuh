@@ -23,6 +23,7 @@ cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
 cudaError_t init_tc_attrs();
 cudaError_t launch_accum_q_tc(int K, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_p_tc(int K, const PassArgs& a, cudaStream_t st);
+size_t tc_image_bytes(int K, int64_t I, int64_t J);
 
 // decode / checks / synthetic data
 cudaError_t launch_pack(const uint8_t* bed, int64_t bps, int64_t I, int64_t J, int64_t Ipad, int JW, uint32_t* G,

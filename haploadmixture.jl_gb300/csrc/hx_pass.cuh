@@ -46,6 +46,7 @@ struct PassArgs {
     double* XtX;            // direct outputs when S == 1 (P side)
     double* Xtz;
     double* slots;          // per-context scalar block (tensor-core kernels record timeouts there)
+    uint8_t* img;           // tensor-core passes: B-operand image of the pass (written by the pass)
 };
 
 template <int K> __device__ __forceinline__ constexpr int tri(int k, int k2) {
