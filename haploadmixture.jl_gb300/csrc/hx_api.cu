@@ -158,10 +158,11 @@ PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
 
 int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, double* Xtz) {
     PassArgs a = pass_args(c, q, p);
-    if (hess && c->tc) {
+    // the gradient-only (EM) Q pass is as fast on the CUDA cores
+    if (c->tc && hess) {
         a.S = c->S_qt; a.per_chunk = c->wpc_qt; a.part = c->part_q;
-        HX_LAUNCH(HX_KIND_ACCUM_Q, 2, launch_accum_q_tc(c->K, a, c->st));
-        HX_LAUNCH(HX_KIND_OTHER, 1, launch_reduce_sym(c->part_q, c->S_qt, c->K, true, c->I, c->Ipad, XtX, Xtz, c->st));
+        HX_LAUNCH(HX_KIND_ACCUM_Q, 2, launch_accum_q_tc(c->K, hess, a, c->st));
+        HX_LAUNCH(HX_KIND_OTHER, 1, launch_reduce_sym(c->part_q, c->S_qt, c->K, hess, c->I, c->Ipad, XtX, Xtz, c->st));
         return HX_OK;
     }
     a.S = c->S_q; a.per_chunk = c->wpc_q; a.part = c->part_q;
@@ -174,12 +175,12 @@ int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
 
 int pass_p(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, double* Xtz) {
     PassArgs a = pass_args(c, q, p);
-    if (hess && c->tc) {
+    if (c->tc) {
         a.S = c->S_pt; a.per_chunk = c->ipc_pt; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;
-        HX_LAUNCH(HX_KIND_ACCUM_P, 2, launch_accum_p_tc(c->K, a, c->st));
+        HX_LAUNCH(HX_KIND_ACCUM_P, 2, launch_accum_p_tc(c->K, hess, a, c->st));
         if (c->S_pt > 1)
             HX_LAUNCH(HX_KIND_OTHER, 1,
-                      launch_reduce_sym(c->part_p, c->S_pt, c->K, true, 4 * c->J, 4 * c->J, XtX, Xtz, c->st));
+                      launch_reduce_sym(c->part_p, c->S_pt, c->K, hess, 4 * c->J, 4 * c->J, XtX, Xtz, c->st));
         return HX_OK;
     }
     a.S = c->S_p; a.per_chunk = c->ipc_p; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;

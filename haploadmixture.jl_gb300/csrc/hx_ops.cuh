@@ -20,9 +20,26 @@ cudaError_t launch_accum_p_f32(int K, bool hess, const PassArgs& a, cudaStream_t
 cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
 
 // tensor-core (tcgen05) Hessian+gradient passes of the mixed method (hx_tc.cu)
+// Host operations on the tensor-core instantiation of one K (hx_tc_impl.cuh);
+// each hx_tc_g*.cu unit serves a few values of K.
+enum TcOp { TC_ATTRS, TC_IMG_BYTES, TC_Q, TC_P };
+struct TcCall {
+    TcOp op;
+    int K;
+    bool hess;
+    const PassArgs* a;
+    cudaStream_t st;
+    int64_t I, J;
+    size_t bytes;
+};
+cudaError_t tc_run_g1(TcCall& c);   // K = 1..7
+cudaError_t tc_run_g2(TcCall& c);   // K = 8, 9
+cudaError_t tc_run_g3(TcCall& c);   // K = 10
+cudaError_t tc_run_g4(TcCall& c);   // K = 11
+cudaError_t tc_run_g5(TcCall& c);   // K = 12
 cudaError_t init_tc_attrs();
-cudaError_t launch_accum_q_tc(int K, const PassArgs& a, cudaStream_t st);
-cudaError_t launch_accum_p_tc(int K, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_accum_q_tc(int K, bool hess, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_accum_p_tc(int K, bool hess, const PassArgs& a, cudaStream_t st);
 size_t tc_image_bytes(int K, int64_t I, int64_t J);
 
 // decode / checks / synthetic data

@@ -1,0 +1,838 @@
+// hx_tc_impl.cuh -- tensor-core (tcgen05) gradient/Hessian passes of the mixed method.
+//
+// Included by the hx_tc_g*.cu translation units, each of which instantiates
+// the kernels for a few values of K (see tc_run); hx_tc.cu dispatches on K.
+//
+// Both accumulations are GEMMs whose A operand is generated on the fly from the
+// genotype classes:
+//   Q side (src/loops.jl:328-365):  H_i = sum_m W[i,m] PP[m,:],  g_i = sum_m U[i,m] P[m,:]
+//   P side (src/loops.jl:367-403):  H_m = sum_i W[i,m] QQ[i,:],  g_m = sum_i U[i,m] Q[i,:]
+// with m = 4j+h, U = c_h/qp_h, W = c_h/qp_h^2, PP[m,(k,k2)] = p[k,m] p[k2,m]
+// (upper triangle) and QQ[i,(k,k2)] = q[k,i] q[k2,i].  The CUDA cores evaluate
+// each (individual, block) pair once (qp, class, U, W) and write 16-bit hi/lo
+// splits of U and W into shared memory; one thread issues
+// tcgen05.mma kind::f16 (16-bit x 16-bit -> fp32 in TMEM) for hi*hi + hi*lo + lo*hi.
+// The Hessian operands use BF16 (8-bit exponent) because W spans ~1 .. 2e10,
+// beyond FP16's range: hi+lo carries 16 significant bits.  The gradient
+// operands use IEEE FP16 hi/lo (22 bits) under exact power-of-two scaling,
+// since the gradient fixes the optimum and the Hessian only the step.
+// TMEM accumulates FP32 over windows of TC_FLUSH stages; each window is folded
+// into registers (the gradient Kahan-compensated), and chunk partials are
+// summed in FP64 by the same reduction as the CUDA-core pass.
+//
+// Operand images.  The B operands depend only on p (Q side) or only on q (P
+// side), so a small kernel writes them once per pass into global memory, in the
+// exact shared-memory core-matrix layout of one stage: for each word column
+// (8 blocks) the PP/P hi/lo tile and the tf32 p tile of the qp MMA; for each
+// group of 32 individuals the QQ/Q hi/lo tile and the FP32 q rows.  The main
+// kernels stream one image slice plus the stage's class words per stage with
+// 1-D bulk copies (TMA engine) into a RING-deep shared-memory ring, completing
+// on an mbarrier with a transaction count.
+//
+// Pipeline per stage, with no CTA-wide barrier in the loop: every thread waits
+// for the stage's ring slot, waits until the MMAs that last read its A buffer
+// (stage s-2) are done, generates its part of the A tiles and arrives on a
+// shared counter; the last arriver issues the stage's MMAs, commits them to an
+// mbarrier, and refills the ring slot of stage s-1 once that stage's MMAs are
+// done.  Warps therefore run up to two stages apart, and two CTAs (16 warps)
+// share an SM.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
+// slots[S_TC_TIMEOUT] and the CTA drains and exits.
+#pragma once
+#include <algorithm>
+#include "hx_ops.cuh"
+#include "hx_tc.cuh"
+
+namespace hx {
+namespace {
+using namespace tc;
+
+constexpr int TC_THREADS = 256;
+constexpr int TC_FLUSH = 8;                // stages per TMEM window (256 reduction indices)
+constexpr long long TC_BUDGET = 4000000000LL;
+constexpr int RING = 3;                    // stage-input ring depth
+constexpr int KD = 32;                     // reduction indices per stage
+constexpr int LBO_STD = 128;
+constexpr int SBO_STD = (KD / 8) * LBO_STD;      // 512
+constexpr int LBO_PAD = 144;               // P-side A: padded for conflict-free generator stores
+constexpr int SBO_PAD = (KD / 8) * LBO_PAD;      // 576
+constexpr int A_TILE_STD = 16 * SBO_STD;   // 128 rows x 32 x 2 B = 8 KB
+constexpr int A_TILE_PAD = 16 * SBO_PAD;
+// Gradient operands: IEEE FP16 hi/lo under exact power-of-two scaling that keeps
+// them in FP16's normal range: U * 2^-2 <= 5e4 (U = c/qp <= 2/1e-5); P or Q * 2^12
+// in [0.04, 4096].
+constexpr float U_SCALE = 0.25f;
+constexpr float GB_SCALE = 4096.0f;
+constexpr double G_UNSCALE = 1.0 / 1024.0;
+
+template <int K> struct TcDims {
+    static constexpr int NH = K * (K + 1) / 2;
+    static constexpr int NHP = (NH + 15) / 16 * 16;
+    static constexpr int NG = 16;
+    static constexpr int NT = NHP + NG;
+    static constexpr int TCOLS = (2 * NT <= 32) ? 32 : (2 * NT <= 64) ? 64 : (2 * NT <= 128) ? 128 : 256;
+    static constexpr int HALF = NT / 2;
+    static constexpr int B_TILE = (NT / 8) * SBO_STD;    // NT rows x 32 x 2 B
+    // CTAs per SM: 2 while the generators fit in 128 registers, else 1
+    static constexpr int MINB = K <= 8 ? 2 : 1;
+};
+
+// qp of the Q side from the tensor core (kind::tf32), see k_accum_q_tc.
+template <int K> struct QpDims {
+    static constexpr int KP = K <= 8 ? 8 : 16;        // reduction padded to tf32 steps of 8
+    static constexpr int SBO = (KP / 4) * 128;        // 4 tf32 per 16-byte core row
+    static constexpr int A_T = 16 * SBO;              // 128 rows
+    static constexpr int B_T = 4 * SBO;               // 32 rows
+    static constexpr int NCOL = 2 * TcDims<K>::NT + 64;
+    static constexpr int TCOLS = NCOL <= 32 ? 32 : NCOL <= 64 ? 64 : NCOL <= 128 ? 128 : 256;
+};
+
+// P side: staged q rows have stride QSTR floats (an odd number of 16-byte
+// units) and individual ii = 4*ig + e sits in row slot 8e + ig, so the 8
+// individual groups ig of a warp read 8 distinct bank quads.
+template <int K> constexpr int qstr() { return K <= 4 ? 4 : 12; }
+__host__ __device__ constexpr int qrow_slot(int ii) { return 8 * (ii & 3) + (ii >> 2); }
+
+// Image bytes per stage: Q side per word column, P side per 32 individuals.
+template <int K> constexpr int qimg_bytes() { return 2 * TcDims<K>::B_TILE + 2 * QpDims<K>::B_T; }
+template <int K> constexpr int pimg_bytes() { return 2 * TcDims<K>::B_TILE + KD * qstr<K>() * 4; }
+
+struct Sync {
+    uint64_t full[RING];   // stage inputs landed (transaction-count barrier)
+    uint64_t mma_done[2];
+    uint64_t flush_done[2];
+    uint64_t qp_done[2];
+    uint32_t tslot;
+    int bad;
+    int issued;            // stages whose MMAs have been issued
+    int loaded;            // stages whose input copies have been issued
+    uint32_t arrived[2];   // generator arrivals on stage buffer b (monotonic)
+    // stage-input sources, read only by the thread that issues a refill
+    const uint8_t* img0;   // image slice of stage 0
+    const uint32_t* g0;    // class words of stage 0
+    int64_t gstride;       // words between word columns (Ipad)
+    int nwc;               // word columns (P side)
+    uint32_t tx;           // bytes per stage
+};
+
+__device__ __forceinline__ bool is_bad(const Sync* sy) { return *(volatile const int*)&sy->bad != 0; }
+
+// Arrival on the stage buffer: returns true for the last of the TC_THREADS
+// generator threads of this use of the buffer (the counter only grows, so no
+// reset races with the next use).  Release/acquire ordering (after each
+// writer's fence.proxy.async) makes every thread's tile stores visible to the
+// MMAs that the last arriver issues.
+__device__ __forceinline__ bool arrive_last(uint32_t* ctr) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;" : "=r"(old) : "r"(smem_u32(ctr)) : "memory");
+    return (old % TC_THREADS) == TC_THREADS - 1;
+}
+
+__device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
+    *(volatile int*)&sy->bad = 1;
+    if (slots) slots[S_TC_TIMEOUT] = 1.0;
+}
+
+// After a timeout: wait (bounded) until the MMAs of the last two issued stages
+// and the bulk copies of the last RING loaded stages have completed, so that
+// TMEM and shared memory are not released under them.  Only operations that
+// were issued are waited for, so each wait ends as soon as the hardware does.
+__device__ __forceinline__ void drain(Sync* sy) {
+    __syncthreads();
+    if (!is_bad(sy)) return;
+    const int n = sy->issued, l = sy->loaded;
+    for (int s = (n >= 2 ? n - 2 : 0); s < n; ++s) mbar_wait(&sy->mma_done[s & 1], (s >> 1) & 1, TC_BUDGET);
+    for (int s = (l >= RING ? l - RING : 0); s < l; ++s) mbar_wait(&sy->full[s % RING], (s / RING) & 1, TC_BUDGET);
+}
+
+// TMEM window fold: this thread's lane, columns [HF*HALF, HF*HALF + HALF) of the
+// accumulator at column base dcol.  Hessian columns add plainly; gradient
+// columns (>= NHP) use Kahan compensation in comp[col - NHP].
+template <int K, int HF>
+__device__ __forceinline__ void fold(uint32_t taddr_lane, int dcol, float* acc, float* comp) {
+    using D = TcDims<K>;
+#pragma unroll
+    for (int c = 0; c < D::HALF / 8; ++c) {
+        float v[8];
+        tmem_ld8(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), v);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int col = HF * D::HALF + 8 * c + t;
+            if (col >= D::NHP) {
+                const float y = v[t] - comp[col - D::NHP];
+                const float s = acc[8 * c + t] + y;
+                comp[col - D::NHP] = (s - acc[8 * c + t]) - y;
+                acc[8 * c + t] = s;
+            } else {
+                acc[8 * c + t] += v[t];
+            }
+        }
+    }
+}
+template <int K>
+__device__ __forceinline__ void fold_half(int hf, uint32_t taddr_lane, int dcol, float* acc, float* comp) {
+    if (hf == 0) fold<K, 0>(taddr_lane, dcol, acc, comp);
+    else fold<K, 1>(taddr_lane, dcol, acc, comp);
+}
+// Applies the Kahan compensation to the gradient columns: acc then holds the sums.
+template <int K, int HF>
+__device__ __forceinline__ void compensate(float* acc, const float* comp) {
+    using D = TcDims<K>;
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) {
+        const int col = HF * D::HALF + c;
+        if (col >= D::NHP) acc[c] -= comp[col - D::NHP];
+    }
+}
+
+// Issues the 3 split products of one 32-deep stage into D (TMEM cols dcol..):
+// Hessian (N = NHP, bf16) and gradient (N = 16, fp16).  A tiles W_hi, W_lo,
+// U_hi, U_lo at aBase + t*aStride; B tiles: hi at bBase, lo at bBase + B_TILE.
+template <int K, bool HESS>
+__device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aBase, int aStride, int aLBO, int aSBO,
+                                            uint32_t bBase, bool first) {
+    using D = TcDims<K>;
+    constexpr uint32_t idH = idesc_bf16(D::NHP);
+    constexpr uint32_t idG = idesc_f16(D::NG);
+    const uint32_t dH = tmem + dcol;
+    const uint32_t dG = tmem + dcol + D::NHP;
+    const uint32_t bPPh = bBase, bPPl = bBase + D::B_TILE;
+    const uint32_t bPh = bBase + (D::NHP / 8) * SBO_STD, bPl = bPh + D::B_TILE;
+#pragma unroll
+    for (int ks = 0; ks < KD / 16; ++ks) {
+        const uint32_t ao = ks * 2 * aLBO, bo = ks * 2 * LBO_STD;
+        const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
+        const uint64_t aWh = sdesc(aBase + ao, aLBO, aSBO), aWl = sdesc(aBase + aStride + ao, aLBO, aSBO);
+        const uint64_t aUh = sdesc(aBase + 2 * aStride + ao, aLBO, aSBO), aUl = sdesc(aBase + 3 * aStride + ao, aLBO, aSBO);
+        if (HESS) {
+            mma_bf16(dH, aWh, sdesc(bPPh + bo, LBO_STD, SBO_STD), idH, acc0);
+            mma_bf16(dH, aWh, sdesc(bPPl + bo, LBO_STD, SBO_STD), idH, 1u);
+            mma_bf16(dH, aWl, sdesc(bPPh + bo, LBO_STD, SBO_STD), idH, 1u);
+        }
+        mma_bf16(dG, aUh, sdesc(bPh + bo, LBO_STD, SBO_STD), idG, acc0);
+        mma_bf16(dG, aUh, sdesc(bPl + bo, LBO_STD, SBO_STD), idG, 1u);
+        mma_bf16(dG, aUl, sdesc(bPh + bo, LBO_STD, SBO_STD), idG, 1u);
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void issue_qp(uint32_t tmem_col, uint32_t sAq, uint32_t sBq_buf) {
+    using QD = QpDims<K>;
+    constexpr uint32_t id = idesc_tf32(32);
+#pragma unroll
+    for (int ks = 0; ks < QD::KP / 8; ++ks) {
+        const uint32_t o = ks * 256;
+        const uint64_t ah = sdesc(sAq + o, 128, QD::SBO), al = sdesc(sAq + QD::A_T + o, 128, QD::SBO);
+        const uint64_t bh = sdesc(sBq_buf + o, 128, QD::SBO), bl = sdesc(sBq_buf + QD::B_T + o, 128, QD::SBO);
+        mma_tf32(tmem_col, ah, bh, id, ks > 0 ? 1u : 0u);
+        mma_tf32(tmem_col, ah, bl, id, 1u);
+        mma_tf32(tmem_col, al, bh, id, 1u);
+    }
+}
+
+// ------------------------------------------------------------------ images
+// B tile rows of one 8-deep reduction group kg from the 8 K-vectors v[e]
+// (e = reduction index within the group): rows n < NH are the products
+// v[k] v[k2] (bf16 hi/lo), rows NHP.. NHP+K-1 the scaled vector (fp16 hi/lo),
+// other rows zero.  Row n's 16-byte hi chunk goes to
+// base + (n/8)*SBO + kg*LBO + (n%8)*16, the lo chunk B_TILE further.
+template <int K>
+__device__ __forceinline__ void put_b_row(uint8_t* base, int kg, int n, const uint32_t (&h)[4], const uint32_t (&l)[4]) {
+    uint8_t* d = base + (n >> 3) * SBO_STD + kg * LBO_STD + (n & 7) * 16;
+    *reinterpret_cast<uint4*>(d) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(d + TcDims<K>::B_TILE) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+template <int K>
+__device__ __forceinline__ void write_b_rows(const float (&v)[8][K], uint8_t* base, int kg) {
+    using D = TcDims<K>;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int k2 = k; k2 < K; ++k2) {
+            uint32_t h[4], l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                split2(v[2 * e][k] * v[2 * e][k2], v[2 * e + 1][k] * v[2 * e + 1][k2], h[e], l[e]);
+            put_b_row<K>(base, kg, tri_idx<K>(k, k2), h, l);
+        }
+    }
+    const uint32_t z[4] = {0u, 0u, 0u, 0u};
+    for (int n = D::NH; n < D::NHP; ++n) put_b_row<K>(base, kg, n, z, z);
+#pragma unroll
+    for (int kk = 0; kk < D::NG; ++kk) {
+        uint32_t h[4], l[4];
+        const int kc = kk < K ? kk : 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float a0 = kk < K ? v[2 * e][kc] * GB_SCALE : 0.f;
+            const float a1 = kk < K ? v[2 * e + 1][kc] * GB_SCALE : 0.f;
+            split2_f16(a0, a1, h[e], l[e]);
+        }
+        put_b_row<K>(base, kg, D::NHP + kk, h, l);
+    }
+}
+
+// Q-side image of word column jw (blocks 8jw..8jw+7, haplotype columns
+// m = 32jw..32jw+31); thread (jw, kg) covers columns 8kg..8kg+7 of it.
+// Columns past 4J read p = 0.25 (their class nibbles are padding).
+template <int K>
+__global__ void __launch_bounds__(128) k_qimg(const double* __restrict__ p, int64_t J, int JW, uint8_t* __restrict__ img) {
+    using QD = QpDims<K>;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)JW * 4) return;
+    const int64_t jw = t >> 2;
+    const int kg = (int)(t & 3);
+    uint8_t* base = img + jw * qimg_bytes<K>();
+    const int64_t plimit = J * 4 * K;
+    float v[8][K];
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int64_t g = (32 * jw + 8 * kg + e) * K + k;
+            v[e][k] = g < plimit ? (float)p[g] : 0.25f;
+        }
+    write_b_rows<K>(v, base, kg);
+    // tf32 hi/lo p tile of the qp MMA: rows m (32), reduction k (KP, zero-padded)
+    uint8_t* bq = base + 2 * TcDims<K>::B_TILE;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int m = 8 * kg + e;
+#pragma unroll
+        for (int k = 0; k < QD::KP; ++k) {
+            const float x = k < K ? v[e][k < K ? k : 0] : 0.f;
+            const float hi = tf32_round(x), lo = tf32_round(x - hi);
+            const int off = (m >> 3) * QD::SBO + (k >> 2) * 128 + (m & 7) * 16 + (k & 3) * 4;
+            *reinterpret_cast<float*>(bq + off) = hi;
+            *reinterpret_cast<float*>(bq + QD::B_T + off) = lo;
+        }
+    }
+}
+
+// P-side image of the 32 individuals of group g; thread (g, kg) covers
+// individuals 32g + 8kg .. +7.  Individuals past I read q = 1/K (their class
+// nibbles are padding).
+template <int K>
+__global__ void __launch_bounds__(128) k_pimg(const double* __restrict__ q, int64_t I, uint8_t* __restrict__ img) {
+    constexpr int QSTR = qstr<K>();
+    const int64_t ng = (I + KD - 1) / KD;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ng * 4) return;
+    const int64_t g = t >> 2;
+    const int kg = (int)(t & 3);
+    uint8_t* base = img + g * pimg_bytes<K>();
+    float v[8][K];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int64_t i = KD * g + 8 * kg + e;
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[e][k] = i < I ? (float)q[(int64_t)K * i + k] : 1.f / K;
+    }
+    write_b_rows<K>(v, base, kg);
+    float* rows = reinterpret_cast<float*>(base + 2 * TcDims<K>::B_TILE);
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+#pragma unroll
+        for (int k = 0; k < QSTR; ++k) rows[qrow_slot(8 * kg + e) * QSTR + k] = k < K ? v[e][k < K ? k : 0] : 0.f;
+}
+
+// ------------------------------------------------------------------ shared helpers
+__device__ __forceinline__ void init_sync(Sync* sy, int tid) {
+    if (tid == 0) {
+        for (int r = 0; r < RING; ++r) mbar_init(&sy->full[r], 1);
+        mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
+        mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
+        mbar_init(&sy->qp_done[0], 1); mbar_init(&sy->qp_done[1], 1);
+        sy->bad = 0;
+        sy->issued = 0;
+        sy->loaded = 0;
+        sy->arrived[0] = 0;
+        sy->arrived[1] = 0;
+        mbar_fence_init();
+    }
+}
+
+__device__ __forceinline__ void expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(smem_u32(mbar)) : "memory");
+}
+
+// Window bookkeeping after a stage's MMAs were issued by this thread.
+__device__ __forceinline__ void commit_stage(Sync* sy, int s, int ns, int b) {
+    const int d = (s / TC_FLUSH) & 1;
+    commit(&sy->mma_done[b]);
+    if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
+    sy->issued = s + 1;
+}
+
+// Fold of TMEM window w at stage (w+1)*TC_FLUSH + FOLD_OFF: half a window
+// after its last MMAs were issued, so that they are done and no warp waits,
+// and before window w+2 reuses its columns (issued at stage (w+2)*TC_FLUSH,
+// once every thread has arrived there).
+constexpr int FOLD_OFF = TC_FLUSH / 2;
+template <int K>
+__device__ __forceinline__ void maybe_fold(Sync* sy, double* slots, int hf, int s, uint32_t taddr_lane, float* acc,
+                                           float* comp) {
+    using D = TcDims<K>;
+    if (s >= TC_FLUSH + FOLD_OFF && (s - FOLD_OFF) % TC_FLUSH == 0) {
+        const int wp = (s - FOLD_OFF) / TC_FLUSH - 1;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
+        if (!ok) set_bad(sy, slots);
+        else {
+            fence_after();
+            fold_half<K>(hf, taddr_lane, (wp & 1) * D::NT, acc, comp);
+        }
+        fence_before();
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int ns, uint32_t taddr_lane, float* acc,
+                                           float* comp) {
+    using D = TcDims<K>;
+    __syncthreads();
+    if (ns > 0 && !is_bad(sy)) {
+        // windows not folded in the loop: the last one and possibly the one before
+        const int wl = (ns - 1) / TC_FLUSH;
+        const int nf = ns - 1 >= FOLD_OFF ? (ns - 1 - FOLD_OFF) / TC_FLUSH : 0;
+        for (int w = nf; w <= wl; ++w) {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[w & 1], (w >> 1) & 1, TC_BUDGET));
+            if (!ok) { set_bad(sy, slots); break; }
+            fence_after();
+            fold_half<K>(hf, taddr_lane, (w & 1) * D::NT, acc, comp);
+        }
+    }
+    drain(sy);
+    fence_before();
+    __syncthreads();
+    if (hf == 0) compensate<K, 0>(acc, comp);
+    else compensate<K, 1>(acc, comp);
+}
+
+// ------------------------------------------------------------------ Q side
+// CTA: 128 individuals (TMEM lanes) x a chunk of class words; stage = 1 word
+// (8 blocks, 32 haplotype columns).  Thread (r, hf): row r, blocks 4hf..4hf+3.
+// qp[i, m] = sum_k q[k,i] p[k,m] also comes from the tensor core: kind::tf32
+// MMAs (hi*hi + hi*lo + lo*hi of TF32-rounded splits, ~2^-21 relative) of the
+// CTA's q tile by the stage's p tile into a double-buffered 32-column TMEM
+// tile, issued one stage ahead; each thread reads its row's 16 values.
+
+// One pair from its qp: U (scaled) and W.
+template <bool HESS>
+__device__ __forceinline__ void gen_pair_qp(unsigned nib, const float* qp, float* U4, float* W4, const float4* tab) {
+    float L, u[4];
+    pair_eval_tab(nib, qp, L, u, tab);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        U4[h] = u[h] * U_SCALE;
+        if (HESS) W4[h] = u[h] * rcp_approx(qp[h]);
+    }
+}
+
+template <int K, bool HESS>
+__global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(PassArgs a) {
+    using D = TcDims<K>;
+    using QD = QpDims<K>;
+    constexpr int GB = qimg_bytes<K>();
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_STD]
+    const uint32_t sAq = sA + 2 * 4 * A_TILE_STD;                    // [2 hi/lo][A_T]
+    const uint32_t sR = sAq + 2 * QD::A_T;                           // ring [RING][GB]
+    uint32_t* SW = (uint32_t*)(smem + (sR - sA) + RING * GB);        // [RING][128]
+    Sync* sy = (Sync*)(SW + RING * 128);
+    __shared__ float4 s_snp[4];
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = tid & 127, hf = tid >> 7;
+    const int64_t i = (int64_t)blockIdx.x * 128 + r;
+    const bool active = i < a.I;
+    const int w0 = blockIdx.y * a.per_chunk;
+    const int ns = min(a.JW, w0 + a.per_chunk) - w0;     // one word per stage
+    const int64_t i0 = (int64_t)blockIdx.x * 128;
+    snp_table_init(s_snp, tid);
+
+    // stage t's inputs: the word column's image and the CTA's 128 class words
+    auto load_stage = [&](int t) {
+        const int slot = t % RING;
+        expect_tx(&sy->full[slot], (uint32_t)(GB + 512));
+        bulk_copy(sR + slot * GB, sy->img0 + (int64_t)t * GB, GB, &sy->full[slot]);
+        bulk_copy(smem_u32(SW + slot * 128), sy->g0 + (int64_t)t * sy->gstride, 512, &sy->full[slot]);
+        sy->loaded = t + 1;
+    };
+
+    if (warp == 0) tmem_alloc<QD::TCOLS>(&sy->tslot);
+    init_sync(sy, tid);
+    if (tid == 0) {
+        sy->img0 = a.img + (int64_t)w0 * GB;
+        sy->g0 = a.G + (int64_t)w0 * a.Ipad + i0;
+        sy->gstride = a.Ipad;
+    }
+    // zero the q tile (reduction padding k >= K stays zero)
+    for (int t = tid; t < (2 * QD::A_T) / 4; t += TC_THREADS)
+        asm volatile("st.shared.b32 [%0], %1;" :: "r"(sAq + 4 * t), "r"(0u) : "memory");
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sy->tslot;
+    const uint32_t tq = tmem + 2 * D::NT;                 // qp tiles: columns [2NT, 2NT + 64)
+    const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    if (tid == 0)
+        for (int t = 0; t < RING && t < ns; ++t) load_stage(t);
+
+    // q tile (tf32 hi/lo), once per CTA
+    if (hf == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float x = active ? (float)a.q[(int64_t)K * i + k] : 1.f / K;
+            const float hi = tf32_round(x), lo = tf32_round(x - hi);
+            const uint32_t off = (r >> 3) * QD::SBO + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4;
+            asm volatile("st.shared.b32 [%0], %1;" :: "r"(sAq + off), "f"(hi) : "memory");
+            asm volatile("st.shared.b32 [%0], %1;" :: "r"(sAq + QD::A_T + off), "f"(lo) : "memory");
+        }
+    }
+    float acc[D::HALF], comp[D::NG];
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) acc[c] = 0.f;
+#pragma unroll
+    for (int c = 0; c < D::NG; ++c) comp[c] = 0.f;
+
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    if (tid == 0 && ns > 0) {
+        if (!mbar_wait(&sy->full[0], 0, TC_BUDGET)) set_bad(sy, a.slots);
+        else {
+            fence_after();
+            issue_qp<K>(tq, sAq, sR + 2 * D::B_TILE);
+            commit(&sy->qp_done[0]);
+        }
+    }
+
+    for (int s = 0; s < ns; ++s) {
+        const int b = s & 1, bn = b ^ 1, slot = s % RING;
+        if (!mbar_wait(&sy->full[slot], (s / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        // A buffer b was last read by the MMAs of stage s-2
+        if (s >= 2 && !is_bad(sy))
+            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        if (is_bad(sy)) break;
+        const uint32_t word = SW[slot * 128 + r];
+        // this stage's qp: 16 columns of this thread's row
+        float qpv[16];
+        {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], (s >> 1) & 1, TC_BUDGET));
+            if (!ok) { set_bad(sy, a.slots); break; }
+            fence_after();
+            tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16), qpv);
+            tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16 + 8), qpv + 8);
+        }
+        const uint32_t aB = sA + b * 4 * A_TILE_STD;
+#pragma unroll
+        for (int t2 = 0; t2 < 2; ++t2) {
+            float W[8], U[8];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int bb = 2 * t2 + e;                    // block within this thread's half
+                gen_pair_qp<HESS>((word >> (4 * (hf * 4 + bb))) & 0xFu, qpv + 4 * bb, U + 4 * e, W + 4 * e, s_snp);
+            }
+            const uint32_t off = (r >> 3) * SBO_STD + (hf * 2 + t2) * LBO_STD + (r & 7) * 16;
+            uint32_t wh[4], wl[4], uh[4], ul[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (HESS) split2(W[2 * e], W[2 * e + 1], wh[e], wl[e]);
+                split2_f16(U[2 * e], U[2 * e + 1], uh[e], ul[e]);
+            }
+            if (HESS) {
+                sts128(aB + off, wh[0], wh[1], wh[2], wh[3]);
+                sts128(aB + A_TILE_STD + off, wl[0], wl[1], wl[2], wl[3]);
+            }
+            sts128(aB + 2 * A_TILE_STD + off, uh[0], uh[1], uh[2], uh[3]);
+            sts128(aB + 3 * A_TILE_STD + off, ul[0], ul[1], ul[2], ul[3]);
+        }
+        fence_async_smem();
+        fence_before();
+        if (arrive_last(&sy->arrived[b])) {
+            fence_after();
+            // the next stage's qp first, so that it does not queue behind this stage's MMAs
+            if (s + 1 < ns) {
+                const int sn = (s + 1) % RING;
+                if (!mbar_wait(&sy->full[sn], ((s + 1) / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+                else {
+                    issue_qp<K>(tq + bn * 32, sAq, sR + sn * GB + 2 * D::B_TILE);
+                    commit(&sy->qp_done[bn]);
+                }
+            }
+            const int d = (s / TC_FLUSH) & 1;
+            issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GB, (s % TC_FLUSH) == 0);
+            // mma_done also covers the qp MMA, so that draining it covers every MMA in flight
+            commit_stage(sy, s, ns, b);
+            // refill the slot of stage s-1 once its MMAs are done (its qp MMA was
+            // issued before them)
+            if (s >= 1 && s - 1 + RING < ns) {
+                if (!mbar_wait(&sy->mma_done[(s - 1) & 1], ((s - 1) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+                else load_stage(s - 1 + RING);
+            }
+        }
+        maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
+    }
+    final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
+    // write partials: v < K gradient, v = K + tri index Hessian
+    constexpr int NV = K + (HESS ? D::NH : 0);
+    double* out = a.part + (int64_t)blockIdx.y * NV * a.Ipad;
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) {
+        const int col = hf * D::HALF + c;
+        if (col < D::NH) {
+            if (HESS) out[(int64_t)(K + col) * a.Ipad + i] = (double)acc[c];
+        } else if (col >= D::NHP && col < D::NHP + K) {
+            out[(int64_t)(col - D::NHP) * a.Ipad + i] = (double)acc[c] * G_UNSCALE;
+        }
+    }
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc<QD::TCOLS>(tmem);
+    }
+}
+
+// ------------------------------------------------------------------ P side
+// CTA: 32 blocks (128 haplotype columns = TMEM lanes) x a chunk of individuals;
+// stage = 32 individuals.  Thread (jl, ig): block jl, individuals 4ig..4ig+3.
+
+// One (individual, block) pair: qp from q and p (4K values), then U (scaled)
+// and W.
+template <int K, bool HESS>
+__device__ __forceinline__ void gen_pair(unsigned nib, const float* qv, const float* pb, float* U4, float* W4,
+                                         const float4* tab) {
+    float qp[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        float sm = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) sm = fmaf(qv[k], pb[h * K + k], sm);
+        qp[h] = sm;
+    }
+    float L, u[4];
+    pair_eval_tab(nib, qp, L, u, tab);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        U4[h] = u[h] * U_SCALE;
+        if (HESS) W4[h] = u[h] * rcp_approx(qp[h]);
+    }
+}
+
+template <int K, bool HESS>
+__global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(PassArgs a) {
+    using D = TcDims<K>;
+    constexpr int QSTR = qstr<K>();
+    constexpr int GB = pimg_bytes<K>();
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_PAD]
+    const uint32_t sR = sA + 2 * 4 * A_TILE_PAD;                     // ring [RING][GB]
+    uint32_t* SW = (uint32_t*)(smem + (sR - sA) + RING * GB);        // [RING][4][KD]
+    Sync* sy = (Sync*)(SW + RING * 4 * KD);
+    __shared__ float4 s_snp[4];
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int jl = tid >> 3, ig = tid & 7;
+    const int hf = tid >> 7;
+    const int64_t j = (int64_t)blockIdx.x * 32 + jl;
+    const bool valid = j < a.J;
+    const int64_t i0 = (int64_t)blockIdx.y * a.per_chunk;
+    const int64_t i1 = min(a.I, i0 + (int64_t)a.per_chunk);
+    const int ns = (int)((i1 - i0 + KD - 1) / KD);
+    const int64_t g0 = i0 / KD;
+    const int64_t jw0 = (int64_t)blockIdx.x * 4;
+    const int nwc = (int)min((int64_t)4, (int64_t)a.JW - jw0);     // word columns inside the matrix
+    snp_table_init(s_snp, tid);
+
+    // stage t's inputs: the 32 individuals' image and their class words of the
+    // CTA's word columns (columns past JW are never read: their blocks are
+    // past J and evaluate as padding)
+    auto load_stage = [&](int t) {
+        const int slot = t % RING;
+        expect_tx(&sy->full[slot], sy->tx);
+        bulk_copy(sR + slot * GB, sy->img0 + (int64_t)t * GB, GB, &sy->full[slot]);
+        for (int w = 0; w < sy->nwc; ++w)
+            bulk_copy(smem_u32(SW + (slot * 4 + w) * KD), sy->g0 + w * sy->gstride + (int64_t)KD * t, 128,
+                      &sy->full[slot]);
+        sy->loaded = t + 1;
+    };
+
+    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+    init_sync(sy, tid);
+    if (tid == 0) {
+        sy->img0 = a.img + g0 * GB;
+        sy->g0 = a.G + jw0 * a.Ipad + i0;
+        sy->gstride = a.Ipad;
+        sy->nwc = nwc;
+        sy->tx = (uint32_t)(GB + 128 * nwc);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sy->tslot;
+    const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    if (tid == 0)
+        for (int t = 0; t < RING && t < ns; ++t) load_stage(t);
+
+    float pr[4 * K];
+#pragma unroll
+    for (int t = 0; t < 4 * K; ++t) pr[t] = valid ? (float)a.p[(int64_t)K * 4 * j + t] : 0.25f;
+    float acc[D::HALF], comp[D::NG];
+#pragma unroll
+    for (int c = 0; c < D::HALF; ++c) acc[c] = 0.f;
+#pragma unroll
+    for (int c = 0; c < D::NG; ++c) comp[c] = 0.f;
+    const int bsh = 4 * (jl & 7);
+
+    for (int s = 0; s < ns; ++s) {
+        const int b = s & 1, slot = s % RING;
+        if (!mbar_wait(&sy->full[slot], (s / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        if (s >= 2 && !is_bad(sy))
+            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        if (is_bad(sy)) break;
+        const float* Qs = reinterpret_cast<const float*>(smem + (sR - sA) + slot * GB + 2 * D::B_TILE);
+        const uint32_t* Ws = SW + slot * 4 * KD + (jl >> 3) * KD;
+        // A = W^T tile: rows m = 4*jl + h, reduction over the stage's individuals
+        float W[4][4], U[4][4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int ii = ig * 4 + e;
+            const unsigned nib = valid ? (Ws[ii] >> bsh) & 0xFu : HX_PAD_NIBBLE;
+            float qv[(K + 3) / 4 * 4];
+            const float4* q4 = reinterpret_cast<const float4*>(Qs + qrow_slot(ii) * QSTR);
+#pragma unroll
+            for (int c = 0; c < (K + 3) / 4; ++c) {
+                const float4 x = q4[c];
+                qv[4 * c] = x.x; qv[4 * c + 1] = x.y; qv[4 * c + 2] = x.z; qv[4 * c + 3] = x.w;
+            }
+            float u4[4], w4[4];
+            gen_pair<K, HESS>(nib, qv, pr, u4, w4, s_snp);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) { U[h][e] = u4[h]; if (HESS) W[h][e] = w4[h]; }
+        }
+        const uint32_t aB = sA + b * 4 * A_TILE_PAD;
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int m = 4 * jl + h;
+            const uint32_t off = (m >> 3) * SBO_PAD + (ig >> 1) * LBO_PAD + (m & 7) * 16 + (ig & 1) * 8;
+            uint32_t wh[2], wl[2], uh[2], ul[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                if (HESS) split2(W[h][2 * e], W[h][2 * e + 1], wh[e], wl[e]);
+                split2_f16(U[h][2 * e], U[h][2 * e + 1], uh[e], ul[e]);
+            }
+            if (HESS) {
+                asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + off), "r"(wh[0]), "r"(wh[1]) : "memory");
+                asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + A_TILE_PAD + off), "r"(wl[0]), "r"(wl[1]) : "memory");
+            }
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + 2 * A_TILE_PAD + off), "r"(uh[0]), "r"(uh[1]) : "memory");
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + 3 * A_TILE_PAD + off), "r"(ul[0]), "r"(ul[1]) : "memory");
+        }
+        fence_async_smem();
+        fence_before();
+        if (arrive_last(&sy->arrived[b])) {
+            fence_after();
+            const int d = (s / TC_FLUSH) & 1;
+            issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, sR + slot * GB, (s % TC_FLUSH) == 0);
+            commit_stage(sy, s, ns, b);
+            if (s >= 1 && s - 1 + RING < ns) {
+                if (!mbar_wait(&sy->mma_done[(s - 1) & 1], ((s - 1) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+                else load_stage(s - 1 + RING);
+            }
+        }
+        maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
+    }
+    final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
+    // rows m of this CTA: TMEM lane r
+    const int r = tid & 127;
+    const int64_t m = (int64_t)blockIdx.x * 128 + r;
+    if (m < 4 * a.J) {
+        constexpr int NV = K + (HESS ? D::NH : 0);
+        const int64_t rows = 4 * a.J;
+#pragma unroll
+        for (int c = 0; c < D::HALF; ++c) {
+            const int col = hf * D::HALF + c;
+            if (col < D::NH) {
+                if (!HESS) continue;
+                const double val = (double)acc[c];
+                if (a.S == 1) {
+                    int k, k2;
+                    tri_pair<K>(col, k, k2);
+                    a.XtX[(int64_t)K * K * m + k2 + K * k] = val;
+                    a.XtX[(int64_t)K * K * m + k + K * k2] = val;
+                } else {
+                    a.part[((int64_t)blockIdx.y * NV + K + col) * rows + m] = val;
+                }
+            } else if (col >= D::NHP && col < D::NHP + K) {
+                const double val = (double)acc[c] * G_UNSCALE;
+                if (a.S == 1) a.Xtz[(int64_t)K * m + (col - D::NHP)] = val;
+                else a.part[((int64_t)blockIdx.y * NV + (col - D::NHP)) * rows + m] = val;
+            }
+        }
+    }
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc<D::TCOLS>(tmem);
+    }
+}
+
+template <int K> constexpr size_t smem_q() {
+    using QD = QpDims<K>;
+    return 1024 + 2 * 4 * A_TILE_STD + 2 * QD::A_T + RING * qimg_bytes<K>() + RING * 128 * 4 + sizeof(Sync);
+}
+template <int K> constexpr size_t smem_p() {
+    return 1024 + 2 * 4 * A_TILE_PAD + RING * pimg_bytes<K>() + RING * 4 * KD * 4 + sizeof(Sync);
+}
+
+// One entry for every host-side operation on the K instantiation.
+template <int K>
+cudaError_t tc_run(TcCall& c) {
+    switch (c.op) {
+    case TC_ATTRS: {
+        cudaError_t e = cudaFuncSetAttribute(k_accum_q_tc<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem_q<K>());
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_accum_q_tc<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem_q<K>());
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_accum_p_tc<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem_p<K>());
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_accum_p_tc<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem_p<K>());
+        return e;
+    }
+    case TC_IMG_BYTES: {
+        const int64_t JW = (c.J + 7) / 8, ng = (c.I + KD - 1) / KD;
+        c.bytes = std::max((size_t)JW * qimg_bytes<K>(), (size_t)ng * pimg_bytes<K>());
+        return cudaSuccess;
+    }
+    case TC_Q: {   // two launches: the operand image, then the pass
+        const PassArgs& a = *c.a;
+        const unsigned gi = (unsigned)(((int64_t)a.JW * 4 + 127) / 128);
+        dim3 grid((unsigned)(a.Ipad / 128), (unsigned)a.S);
+        k_qimg<K><<<gi, 128, 0, c.st>>>(a.p, a.J, a.JW, a.img);
+        if (c.hess) k_accum_q_tc<K, true><<<grid, TC_THREADS, smem_q<K>(), c.st>>>(a);
+        else k_accum_q_tc<K, false><<<grid, TC_THREADS, smem_q<K>(), c.st>>>(a);
+        return cudaGetLastError();
+    }
+    case TC_P: {
+        const PassArgs& a = *c.a;
+        const unsigned gi = (unsigned)((((a.I + KD - 1) / KD) * 4 + 127) / 128);
+        dim3 grid((unsigned)((a.J + 31) / 32), (unsigned)a.S);
+        k_pimg<K><<<gi, 128, 0, c.st>>>(a.q, a.I, a.img);
+        if (c.hess) k_accum_p_tc<K, true><<<grid, TC_THREADS, smem_p<K>(), c.st>>>(a);
+        else k_accum_p_tc<K, false><<<grid, TC_THREADS, smem_p<K>(), c.st>>>(a);
+        return cudaGetLastError();
+    }
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+}  // namespace hx
