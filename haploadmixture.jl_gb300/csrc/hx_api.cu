@@ -36,6 +36,7 @@ struct hx_ctx {
     double* slots = nullptr;
     double* h_slots = nullptr;   // pinned
     uint8_t* img = nullptr;      // B-operand image of the tensor-core passes
+    int8_t* qp_ws = nullptr;     // P-side QP working sets, warm start of the next solve
     int S_q = 1, wpc_q = 1, S_p = 1, ipc_p = 1;
     bool tc = false;                         // Hessian passes on the tensor cores
     int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
@@ -196,10 +197,15 @@ int pass_p(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
 int loglik_to_slot(hx_ctx* c, const double* q, const double* p, int slot) {
     PassArgs a = pass_args(c, q, p);
     a.S = c->S_q; a.per_chunk = c->wpc_q; a.part = c->part_ll;
-    HX_LAUNCH(HX_KIND_LOGLIK, 1,
-              c->prec == HX_PREC_FP64 ? launch_loglik_f64(c->K, a, c->st) : launch_loglik_f32(c->K, a, c->st));
-    HX_LAUNCH(HX_KIND_OTHER, 1,
-              launch_reduce_sum(c->part_ll, (c->Ipad / ACC_THREADS) * c->S_q, c->slots + slot, c->st));
+    if (c->prec == HX_PREC_FP64) {
+        HX_LAUNCH(HX_KIND_LOGLIK, 1, launch_loglik_f64(c->K, a, c->st));
+        HX_LAUNCH(HX_KIND_OTHER, 1,
+                  launch_reduce_sum(c->part_ll, (c->Ipad / ACC_THREADS) * c->S_q, c->slots + slot, c->st));
+    } else {
+        HX_LAUNCH(HX_KIND_LOGLIK, 1, launch_loglik_f32x2(c->K, a, c->st));
+        HX_LAUNCH(HX_KIND_OTHER, 1,
+                  launch_reduce_sum(c->part_ll, (int64_t)loglik_f32x2_blocks(c->Ipad) * c->S_q, c->slots + slot, c->st));
+    }
     return HX_OK;
 }
 
@@ -245,7 +251,8 @@ int update_p(hx_ctx* c, bool update2) {
     double* p = update2 ? pof(c, c->xn) : pof(c, c->x);
     double* out = update2 ? pof(c, c->xn2) : pof(c, c->xn);
     HX_ST(pass_p(c, q, p, true, c->XtXp, c->Xtzp));
-    HX_LAUNCH(HX_KIND_QP_P, 1, launch_qp_p(c->K, c->J, c->XtXp, c->Xtzp, p, c->rho, pof(c, c->xt), c->slots, c->st));
+    HX_LAUNCH(HX_KIND_QP_P, 1,
+              launch_qp_p(c->K, c->J, c->XtXp, c->Xtzp, p, c->rho, pof(c, c->xt), c->slots, c->qp_ws, c->st));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_p(p, pof(c, c->xt), c->K, c->J, c->eps, out, c->st));
     return HX_OK;
 }
@@ -327,6 +334,8 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));
     if (c->tc) HX_ST(dalloc(c, &c->img, tc_image_bytes(K, I, J)));
+    HX_ST(dalloc(c, &c->qp_ws, (size_t)4 * K * J));
+    HX_CK(cudaMemsetAsync(c->qp_ws, 0, (size_t)4 * K * J, c->st));
     HX_CK(cudaMallocHost((void**)&c->h_slots, HX_NSLOT * sizeof(double)));
     HX_CK(cudaMemsetAsync(c->U, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
     HX_CK(cudaMemsetAsync(c->V, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
@@ -358,6 +367,9 @@ int upload_x(hx_ctx* c, const double* q, const double* p, bool device, double* d
 }
 
 int reset_state(hx_ctx* c) {
+    // a new trajectory starts from cold QP working sets, so that a fit from
+    // given Q, P is reproducible regardless of earlier calls
+    HX_CK(cudaMemsetAsync(c->qp_ws, 0, (size_t)4 * c->K * c->J, c->st));
     HX_CK(cudaMemsetAsync(c->U, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
     HX_CK(cudaMemsetAsync(c->V, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
     HX_CK(cudaStreamSynchronize(c->st));
@@ -427,7 +439,7 @@ int hx_destroy(hx_ctx* c) {
     if (!c) return HX_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     void* bufs[] = {c->G, c->dm, c->x, c->xn, c->xn2, c->xt, c->xio, c->U, c->V, c->XtXq, c->Xtzq, c->XtXp,
-                    c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots, c->img};
+                    c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots, c->img, c->qp_ws};
     for (void* b : bufs) if (b) cudaFree(b);
     prof_resolve(c);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
@@ -600,7 +612,7 @@ int hx_qp_p(hx_ctx* c, int64_t n, const double* XtX, const double* Xtz, const do
     HX_CK(cudaMemcpyAsync(dX, XtX, (size_t)K * K * 4 * n * 8, cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaMemcpyAsync(dz, Xtz, (size_t)K * 4 * n * 8, cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaMemcpyAsync(dp, p, (size_t)K * 4 * n * 8, cudaMemcpyHostToDevice, c->st));
-    HX_CK(launch_qp_p(K, n, dX, dz, dp, c->rho, dd, c->slots, c->st));
+    HX_CK(launch_qp_p(K, n, dX, dz, dp, c->rho, dd, c->slots, nullptr, c->st));
     HX_CK(cudaMemcpyAsync(pdiff, dd, (size_t)K * 4 * n * 8, cudaMemcpyDeviceToHost, c->st));
     HX_CK(cudaStreamSynchronize(c->st));
     return HX_OK;

@@ -246,11 +246,17 @@ __global__ void k_step_p(const double* __restrict__ p, const double* __restrict_
 // block of H is factorised by a warp-parallel right-looking Cholesky in
 // shared memory.  Restates OpenADMIXTURE's create_tableau!/quadratic_program!
 // contract as called at src/algorithms_inner.jl:160-166 and :303-305.
+// GB300's FP64 unit is narrow and every lane's FP64 operation costs issue
+// slots on it, so each scalar step (square root, pivot reciprocal, the
+// solved unknown of a triangular sweep) is computed by lane 0 alone and
+// broadcast; rows then scale by the reciprocal.  The working set may start
+// from a previous solve's final set (box-only problems, where any set is a
+// feasible start): the method converges to the same unique minimiser.
 enum { QF = 0, QL = 1, QH = 2 };
 
 struct QPWork {
     double* A;
-    double *d, *z, *lo, *hi, *r, *y1, *y2, *ds, *g;
+    double *d, *z, *lo, *hi, *r, *y1, *y2, *ds, *g, *iv;
     int *st, *F;
 };
 
@@ -263,19 +269,26 @@ __device__ __forceinline__ double wmax(double v) {
     return v;
 }
 
-__device__ void tri_solve(const double* A, int nF, double* x, int lane) {
+// L L' x = b in place (L lower, iv[a] = 1 / L[a,a]).
+__device__ void tri_solve(const double* A, const double* iv, int nF, double* x, int lane) {
     for (int a = 0; a < nF; ++a) {
         __syncwarp();
-        const double xa = x[a] / A[a + nF * a];
-        __syncwarp();
-        if (lane == 0) x[a] = xa;
+        double xa = 0.0;
+        if (lane == 0) {
+            xa = x[a] * iv[a];
+            x[a] = xa;
+        }
+        xa = __shfl_sync(FULL, xa, 0);
         for (int rr = a + 1 + lane; rr < nF; rr += 32) x[rr] -= A[rr + nF * a] * xa;
     }
     for (int a = nF - 1; a >= 0; --a) {
         __syncwarp();
-        const double xa = x[a] / A[a + nF * a];
-        __syncwarp();
-        if (lane == 0) x[a] = xa;
+        double xa = 0.0;
+        if (lane == 0) {
+            xa = x[a] * iv[a];
+            x[a] = xa;
+        }
+        xa = __shfl_sync(FULL, xa, 0);
         for (int rr = lane; rr < a; rr += 32) x[rr] -= A[a + nF * rr] * xa;
     }
     __syncwarp();
@@ -315,12 +328,17 @@ __device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
             const double fl = 1e-300 + 1e-14 * md;
             for (int c = 0; c < nF; ++c) {
                 __syncwarp();
-                double s = w.A[c + nF * c];
-                if (!(s > fl)) s = fl;
-                const double lcc = sqrt(s);
-                __syncwarp();
-                for (int rr = c + 1 + lane; rr < nF; rr += 32) w.A[rr + nF * c] /= lcc;
-                if (lane == 0) w.A[c + nF * c] = lcc;
+                double inv = 0.0;
+                if (lane == 0) {
+                    double s = w.A[c + nF * c];
+                    if (!(s > fl)) s = fl;
+                    const double lcc = sqrt(s);
+                    inv = 1.0 / lcc;
+                    w.A[c + nF * c] = lcc;
+                    w.iv[c] = inv;
+                }
+                inv = __shfl_sync(FULL, inv, 0);
+                for (int rr = c + 1 + lane; rr < nF; rr += 32) w.A[rr + nF * c] *= inv;
                 __syncwarp();
                 for (int rr = c + 1 + lane; rr < nF; rr += 32) {
                     const double lrc = w.A[rr + nF * c];
@@ -329,10 +347,10 @@ __device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
             }
             __syncwarp();
             for (int a = lane; a < nF; a += 32) w.y1[a] = w.r[a];
-            tri_solve(w.A, nF, w.y1, lane);
+            tri_solve(w.A, w.iv, nF, w.y1, lane);
             if (eq) {
                 for (int a = lane; a < nF; a += 32) w.y2[a] = 1.0;
-                tri_solve(w.A, nF, w.y2, lane);
+                tri_solve(w.A, w.iv, nF, w.y2, lane);
                 double cf = 0.0;
                 for (int b = lane; b < n; b += 32)
                     if (w.st[b] != QF) cf -= w.d[b];
@@ -415,13 +433,13 @@ __device__ QPWork carve(double* base, int nmax) {
     w.A = base;
     double* v = base + nmax * nmax;
     w.d = v; w.z = v + nmax; w.lo = v + 2 * nmax; w.hi = v + 3 * nmax; w.r = v + 4 * nmax;
-    w.y1 = v + 5 * nmax; w.y2 = v + 6 * nmax; w.ds = v + 7 * nmax; w.g = v + 8 * nmax;
-    w.st = reinterpret_cast<int*>(v + 9 * nmax);
+    w.y1 = v + 5 * nmax; w.y2 = v + 6 * nmax; w.ds = v + 7 * nmax; w.g = v + 8 * nmax; w.iv = v + 9 * nmax;
+    w.st = reinterpret_cast<int*>(v + 10 * nmax);
     w.F = w.st + nmax;
     return w;
 }
 __host__ __device__ constexpr size_t qp_warp_bytes(int nmax) {
-    return (size_t)(nmax * nmax + 9 * nmax) * sizeof(double) + (size_t)(2 * nmax) * sizeof(int);
+    return (size_t)(nmax * nmax + 10 * nmax) * sizeof(double) + (size_t)(2 * nmax) * sizeof(int);
 }
 
 struct HQ {
@@ -465,7 +483,7 @@ k_qp_q(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
 
 __global__ void __launch_bounds__(32 * QP_WARPS)
 k_qp_p(int K, int64_t n, const double* __restrict__ XtX, const double* __restrict__ Xtz,
-       const double* __restrict__ p, double rho, double* __restrict__ pdiff, double* slots) {
+       const double* __restrict__ p, double rho, double* __restrict__ pdiff, double* slots, int8_t* __restrict__ ws) {
     extern __shared__ double smem_qp[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t j = (int64_t)blockIdx.x * QP_WARPS + warp;
@@ -478,13 +496,20 @@ k_qp_p(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
         w.z[a] = Xtz[(int64_t)nv * j + a];
         w.lo[a] = 0.0 - pa;
         w.hi[a] = 1.0 - pa;
-        w.st[a] = (w.lo[a] >= 0.0 && w.hi[a] <= 0.0) ? QL : QF;
+        // warm start from the previous solve's working set (bounds only: feasible)
+        int s0 = ws ? (int)ws[(int64_t)nv * j + a] : QF;
+        if (w.lo[a] >= 0.0 && w.hi[a] <= 0.0) s0 = QL;
+        w.st[a] = s0;
+        w.d[a] = s0 == QL ? w.lo[a] : (s0 == QH ? w.hi[a] : 0.0);
     }
     __syncwarp();
     HP H{XtX + (int64_t)K * K * 4 * j, K, rho};
     const int it = warp_qp(nv, false, H, w);
     __syncwarp();
-    for (int a = lane; a < nv; a += 32) pdiff[(int64_t)nv * j + a] = w.d[a];
+    for (int a = lane; a < nv; a += 32) {
+        pdiff[(int64_t)nv * j + a] = w.d[a];
+        if (ws) ws[(int64_t)nv * j + a] = (int8_t)w.st[a];
+    }
     if (it < 0 && lane == 0) atomicAdd(slots + S_QP_FAIL, 1.0);
 }
 
@@ -700,9 +725,9 @@ cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, 
     return cudaGetLastError();
 }
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
-                        double* pdiff, double* slots, cudaStream_t st) {
+                        double* pdiff, double* slots, int8_t* ws, cudaStream_t st) {
     const size_t smem = QP_WARPS * qp_warp_bytes(4 * K);
-    k_qp_p<<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, p, rho, pdiff, slots);
+    k_qp_p<<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, p, rho, pdiff, slots, ws);
     return cudaGetLastError();
 }
 int qn_dots_blocks(int64_t n) {

@@ -18,6 +18,8 @@ cudaError_t launch_loglik_f64(int K, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_q_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_p_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
+cudaError_t launch_loglik_f32x2(int K, const PassArgs& a, cudaStream_t st);   // two individuals per thread
+int loglik_f32x2_blocks(int64_t Ipad);
 
 // tensor-core (tcgen05) Hessian+gradient passes of the mixed method (hx_tc.cu)
 // Host operations on the tensor-core instantiation of one K (hx_tc_impl.cuh);
@@ -72,7 +74,7 @@ cudaError_t init_kernel_attrs();
 cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff,
                         double* slots, cudaStream_t st);
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
-                        double* pdiff, double* slots, cudaStream_t st);
+                        double* pdiff, double* slots, int8_t* ws, cudaStream_t st);
 // ZAL quasi-Newton
 int qn_dots_blocks(int64_t n);
 cudaError_t launch_qn(int64_t n, const double* x, const double* xn, const double* xn2, double* U, double* V,

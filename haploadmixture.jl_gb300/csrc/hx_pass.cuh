@@ -318,4 +318,113 @@ k_loglik(PassArgs a) {
     if (tid == 0) a.part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
 }
 
+// ------------------------------------------------------------------ loglik, FP32
+// The mixed method's log-likelihood pass (same sums as k_loglik<K, float>):
+// each thread carries two individuals (i and i + ACC_THREADS) that share every
+// staged p row, and forms qp for haplotype pairs (h, h+1) with packed FP32x2
+// FMAs (fma.rn.f32x2: two IEEE FMAs per instruction, the same results and
+// order as fmaf).  Stage rows are transposed to [block][k][h] so that one
+// 16-byte load gives p[k, 4j..4j+3].
+__device__ __forceinline__ uint64_t f2_dup(float x) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(d) : "f"(x));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ void f2_split(uint64_t v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+template <int K>
+__global__ void __launch_bounds__(ACC_THREADS)
+k_loglik2(PassArgs a) {
+    __shared__ __align__(16) float spt[QSTAGE_WORDS * 8 * 4 * K];
+    __shared__ double red[ACC_THREADS];
+    __shared__ float4 s_snp[4];
+    const int tid = threadIdx.x;
+    snp_table_init(s_snp, tid);
+    int64_t ii[2];
+    ii[0] = (int64_t)blockIdx.x * 2 * ACC_THREADS + tid;
+    ii[1] = ii[0] + ACC_THREADS;
+    const int w0 = blockIdx.y * a.per_chunk;
+    const int w1 = min(a.JW, w0 + a.per_chunk);
+    uint64_t qd[2][K];
+    float mant[2] = {1.f, 1.f};
+    int ex[2] = {0, 0};
+    bool zero[2] = {false, false}, bad[2] = {false, false};
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            qd[u][k] = f2_dup(ii[u] < a.I ? (float)a.q[(int64_t)K * ii[u] + k] : 1.f / K);
+    for (int ws = w0; ws < w1; ws += QSTAGE_WORDS) {
+        const int nw = min(QSTAGE_WORDS, w1 - ws);
+        uint32_t words[2][QSTAGE_WORDS];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int w = 0; w < QSTAGE_WORDS; ++w)
+                words[u][w] = (w < nw && ii[u] < a.Ipad) ? a.G[(int64_t)(ws + w) * a.Ipad + ii[u]] : HX_PAD_WORD;
+        __syncthreads();
+        const int nval = nw * 8 * 4 * K;
+        const int64_t base = (int64_t)ws * 8 * 4 * K;
+        const int64_t limit = a.J * 4 * K;
+        for (int t = tid; t < nval; t += ACC_THREADS) {
+            const int blk = t / (4 * K), r = t - blk * 4 * K, h = r / K, k = r - h * K;
+            spt[blk * 4 * K + k * 4 + h] = (base + t < limit) ? (float)a.p[base + t] : 0.25f;
+        }
+        __syncthreads();
+        for (int w = 0; w < nw; ++w) {
+#pragma unroll 2
+            for (int b = 0; b < 8; ++b) {
+                const ulonglong2* pb = reinterpret_cast<const ulonglong2*>(spt + (w * 8 + b) * 4 * K);
+                uint64_t z01[2] = {0ull, 0ull}, z23[2] = {0ull, 0ull};
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const ulonglong2 pk = pb[k];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        z01[u] = f2_fma(qd[u][k], pk.x, z01[u]);
+                        z23[u] = f2_fma(qd[u][k], pk.y, z23[u]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const unsigned nib = (words[u][w] >> (4 * b)) & 0xFu;
+                    float qp[4];
+                    f2_split(z01[u], qp[0], qp[1]);
+                    f2_split(z23[u], qp[2], qp[3]);
+                    float L = pair_lik_tab(nib, qp, s_snp);
+                    if (!(L > 0.f)) {
+                        if (L == 0.f) zero[u] = true; else bad[u] = true;
+                        L = 1.f;
+                    }
+                    mant[u] = renorm(mant[u] * L, ex[u]);
+                }
+            }
+        }
+    }
+    double v = 0.0;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        if (ii[u] < a.I) {
+            double x = log((double)mant[u]) + (double)ex[u] * 0.69314718055994530942;
+            if (zero[u]) x = -INFINITY;
+            if (bad[u]) x = NAN;
+            v += x;
+        }
+    }
+    red[tid] = v;
+    __syncthreads();
+    for (int s = ACC_THREADS / 2; s > 0; s >>= 1) {
+        if (tid < s) red[tid] += red[tid + s];
+        __syncthreads();
+    }
+    if (tid == 0) a.part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
 }  // namespace hx
