@@ -182,6 +182,27 @@ __device__ __forceinline__ double pair_lik_t(unsigned nib, const double qp[4], c
     return F1 * F2;
 }
 
+// Packed FP32x2 arithmetic (sm_100+): fma.rn.f32x2 performs two IEEE FMAs,
+// lane by lane, with the results of two fmaf calls.
+__device__ __forceinline__ uint64_t f2_dup(float x) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(d) : "f"(x));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ void f2_split(uint64_t v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
 // Exact exponent/mantissa split used to accumulate products of likelihoods
 // without underflow (one log per thread instead of two per pair).
 __device__ __forceinline__ float renorm(float m, int& e) {

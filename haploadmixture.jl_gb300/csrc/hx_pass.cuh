@@ -325,19 +325,6 @@ k_loglik(PassArgs a) {
 // FMAs (fma.rn.f32x2: two IEEE FMAs per instruction, the same results and
 // order as fmaf).  Stage rows are transposed to [block][k][h] so that one
 // 16-byte load gives p[k, 4j..4j+3].
-__device__ __forceinline__ uint64_t f2_dup(float x) {
-    uint64_t d;
-    asm("mov.b64 %0, {%1, %1};" : "=l"(d) : "f"(x));
-    return d;
-}
-__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ void f2_split(uint64_t v, float& lo, float& hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
 
 template <int K>
 __global__ void __launch_bounds__(ACC_THREADS)

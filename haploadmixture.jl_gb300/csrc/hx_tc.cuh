@@ -106,6 +106,14 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
     for (int t = 0; t < 8; ++t) v[t] = __uint_as_float(r[t]);
 }
 
+// The same load without the wait (several loads, then one tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // x ~= hi + lo with hi, lo bf16 (round to nearest even); returns packed pairs
 // for two values: hi2 = {hi(x0) low half, hi(x1) high half}, lo2 likewise.
 __device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi2, uint32_t& lo2) {

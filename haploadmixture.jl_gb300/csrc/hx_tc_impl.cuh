@@ -50,6 +50,7 @@ constexpr int TC_THREADS = 256;
 constexpr int TC_FLUSH = 8;                // stages per TMEM window (256 reduction indices)
 constexpr long long TC_BUDGET = 4000000000LL;
 constexpr int RING = 3;                    // stage-input ring depth
+constexpr int QRING = 4;                   // Q side: ring of the qp MMA's p tiles, loaded 4 stages ahead
 constexpr int KD = 32;                     // reduction indices per stage
 constexpr int LBO_STD = 128;
 constexpr int SBO_STD = (KD / 8) * LBO_STD;      // 512
@@ -86,10 +87,11 @@ template <int K> struct QpDims {
     static constexpr int TCOLS = NCOL <= 32 ? 32 : NCOL <= 64 ? 64 : NCOL <= 128 ? 128 : 256;
 };
 
-// P side: staged q rows have stride QSTR floats (an odd number of 16-byte
+// P side: staged q rows hold each q[k] twice, (q_k, q_k), as the first operand
+// of packed f32x2 FMAs; rows have stride QSTR floats (an odd number of 16-byte
 // units) and individual ii = 4*ig + e sits in row slot 8e + ig, so the 8
 // individual groups ig of a warp read 8 distinct bank quads.
-template <int K> constexpr int qstr() { return K <= 4 ? 4 : 12; }
+template <int K> constexpr int qstr() { return 4 * ((((2 * K + 3) / 4) | 1)); }
 __host__ __device__ constexpr int qrow_slot(int ii) { return 8 * (ii & 3) + (ii >> 2); }
 
 // Image bytes per stage: Q side per word column, P side per 32 individuals.
@@ -98,6 +100,7 @@ template <int K> constexpr int pimg_bytes() { return 2 * TcDims<K>::B_TILE + KD 
 
 struct Sync {
     uint64_t full[RING];   // stage inputs landed (transaction-count barrier)
+    uint64_t fullq[QRING]; // Q side: p tile of the qp MMA landed
     uint64_t mma_done[2];
     uint64_t flush_done[2];
     uint64_t qp_done[2];
@@ -105,6 +108,7 @@ struct Sync {
     int bad;
     int issued;            // stages whose MMAs have been issued
     int loaded;            // stages whose input copies have been issued
+    int loadedq;           // Q side: stages whose qp p tile copy has been issued
     uint32_t arrived[2];   // generator arrivals on stage buffer b (monotonic)
     // stage-input sources, read only by the thread that issues a refill
     const uint8_t* img0;   // image slice of stage 0
@@ -116,15 +120,21 @@ struct Sync {
 
 __device__ __forceinline__ bool is_bad(const Sync* sy) { return *(volatile const int*)&sy->bad != 0; }
 
-// Arrival on the stage buffer: returns true for the last of the TC_THREADS
-// generator threads of this use of the buffer (the counter only grows, so no
-// reset races with the next use).  Release/acquire ordering (after each
-// writer's fence.proxy.async) makes every thread's tile stores visible to the
-// MMAs that the last arriver issues.
+// Arrival on the stage buffer, one atomic per warp: after __syncwarp (which
+// orders the warp's tile stores, each already fenced to the async proxy), lane
+// 0 adds to the buffer's counter; the lane 0 of the last of the TC_THREADS/32
+// warps of this use of the buffer returns true (the counter only grows, so no
+// reset races with the next use).  Release/acquire ordering of the atomic makes
+// every warp's stores visible to the MMAs that the last arriver issues.
 __device__ __forceinline__ bool arrive_last(uint32_t* ctr) {
-    uint32_t old;
-    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;" : "=r"(old) : "r"(smem_u32(ctr)) : "memory");
-    return (old % TC_THREADS) == TC_THREADS - 1;
+    __syncwarp();
+    bool last = false;
+    if ((threadIdx.x & 31) == 0) {
+        uint32_t old;
+        asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;" : "=r"(old) : "r"(smem_u32(ctr)) : "memory");
+        last = (old % (TC_THREADS / 32)) == TC_THREADS / 32 - 1;
+    }
+    return last;
 }
 
 __device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
@@ -139,9 +149,11 @@ __device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
 __device__ __forceinline__ void drain(Sync* sy) {
     __syncthreads();
     if (!is_bad(sy)) return;
-    const int n = sy->issued, l = sy->loaded;
+    const int n = sy->issued, l = sy->loaded, lq = sy->loadedq;
     for (int s = (n >= 2 ? n - 2 : 0); s < n; ++s) mbar_wait(&sy->mma_done[s & 1], (s >> 1) & 1, TC_BUDGET);
     for (int s = (l >= RING ? l - RING : 0); s < l; ++s) mbar_wait(&sy->full[s % RING], (s / RING) & 1, TC_BUDGET);
+    for (int s = (lq >= QRING ? lq - QRING : 0); s < lq; ++s)
+        mbar_wait(&sy->fullq[s % QRING], (s / QRING) & 1, TC_BUDGET);
 }
 
 // TMEM window fold: this thread's lane, columns [HF*HALF, HF*HALF + HALF) of the
@@ -150,10 +162,15 @@ __device__ __forceinline__ void drain(Sync* sy) {
 template <int K, int HF>
 __device__ __forceinline__ void fold(uint32_t taddr_lane, int dcol, float* acc, float* comp) {
     using D = TcDims<K>;
+    uint32_t raw[D::HALF];
+#pragma unroll
+    for (int c = 0; c < D::HALF / 8; ++c) tmem_ld8_async(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), raw + 8 * c);
+    tmem_wait_ld();
 #pragma unroll
     for (int c = 0; c < D::HALF / 8; ++c) {
         float v[8];
-        tmem_ld8(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), v);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) v[t] = __uint_as_float(raw[8 * c + t]);
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             const int col = HF * D::HALF + 8 * c + t;
@@ -333,13 +350,16 @@ __global__ void __launch_bounds__(128) k_pimg(const double* __restrict__ q, int6
 #pragma unroll
     for (int e = 0; e < 8; ++e)
 #pragma unroll
-        for (int k = 0; k < QSTR; ++k) rows[qrow_slot(8 * kg + e) * QSTR + k] = k < K ? v[e][k < K ? k : 0] : 0.f;
+        for (int k = 0; k < QSTR; ++k)
+            rows[qrow_slot(8 * kg + e) * QSTR + k] = (k >> 1) < K ? v[e][(k >> 1) < K ? (k >> 1) : 0] : 0.f;
 }
 
 // ------------------------------------------------------------------ shared helpers
 __device__ __forceinline__ void init_sync(Sync* sy, int tid) {
     if (tid == 0) {
         for (int r = 0; r < RING; ++r) mbar_init(&sy->full[r], 1);
+        for (int r = 0; r < QRING; ++r) mbar_init(&sy->fullq[r], 1);
+        sy->loadedq = 0;
         mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
         mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
         mbar_init(&sy->qp_done[0], 1); mbar_init(&sy->qp_done[1], 1);
@@ -412,6 +432,18 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int 
     else compensate<K, 1>(acc, comp);
 }
 
+// Ring refill by the stage-s issuer: the slot of stage s-1 receives stage
+// s-1+RING once the MMAs of stage s-1 (issued one stage earlier) are done.
+// Waiting here keeps the copies RING-1 stages ahead of their use; a non-blocking
+// test that defers the refill measured slower.
+template <class LOAD>
+__device__ __forceinline__ void refill_ring(Sync* sy, double* slots, int s, int ns, LOAD&& load_stage) {
+    if (s >= 1 && s - 1 + RING < ns) {
+        if (!mbar_wait(&sy->mma_done[(s - 1) & 1], ((s - 1) >> 1) & 1, TC_BUDGET)) set_bad(sy, slots);
+        else load_stage(s - 1 + RING);
+    }
+}
+
 // ------------------------------------------------------------------ Q side
 // CTA: 128 individuals (TMEM lanes) x a chunk of class words; stage = 1 word
 // (8 blocks, 32 haplotype columns).  Thread (r, hf): row r, blocks 4hf..4hf+3.
@@ -440,9 +472,12 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_STD]
+    constexpr int GBM = 2 * D::B_TILE;                               // main ring slot: the B tile
+    constexpr int GBQ = 2 * QD::B_T;                                 // qp ring slot: tf32 p tile
     const uint32_t sAq = sA + 2 * 4 * A_TILE_STD;                    // [2 hi/lo][A_T]
-    const uint32_t sR = sAq + 2 * QD::A_T;                           // ring [RING][GB]
-    uint32_t* SW = (uint32_t*)(smem + (sR - sA) + RING * GB);        // [RING][128]
+    const uint32_t sR = sAq + 2 * QD::A_T;                           // ring [RING][GBM]
+    const uint32_t sRq = sR + RING * GBM;                            // ring [QRING][GBQ]
+    uint32_t* SW = (uint32_t*)(smem + (sRq - sA) + QRING * GBQ);     // [RING][128]
     Sync* sy = (Sync*)(SW + RING * 128);
     __shared__ float4 s_snp[4];
 
@@ -455,13 +490,20 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     const int64_t i0 = (int64_t)blockIdx.x * 128;
     snp_table_init(s_snp, tid);
 
-    // stage t's inputs: the word column's image and the CTA's 128 class words
+    // stage t's inputs: the word column's B tile and the CTA's 128 class words;
+    // separately, 4 stages ahead, the tf32 p tile of its qp MMA
     auto load_stage = [&](int t) {
         const int slot = t % RING;
-        expect_tx(&sy->full[slot], (uint32_t)(GB + 512));
-        bulk_copy(sR + slot * GB, sy->img0 + (int64_t)t * GB, GB, &sy->full[slot]);
+        expect_tx(&sy->full[slot], (uint32_t)(GBM + 512));
+        bulk_copy(sR + slot * GBM, sy->img0 + (int64_t)t * GB, GBM, &sy->full[slot]);
         bulk_copy(smem_u32(SW + slot * 128), sy->g0 + (int64_t)t * sy->gstride, 512, &sy->full[slot]);
         sy->loaded = t + 1;
+    };
+    auto load_qtile = [&](int t) {
+        const int slot = t % QRING;
+        expect_tx(&sy->fullq[slot], (uint32_t)GBQ);
+        bulk_copy(sRq + slot * GBQ, sy->img0 + (int64_t)t * GB + GBM, GBQ, &sy->fullq[slot]);
+        sy->loadedq = t + 1;
     };
 
     if (warp == 0) tmem_alloc<QD::TCOLS>(&sy->tslot);
@@ -480,8 +522,10 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     const uint32_t tmem = sy->tslot;
     const uint32_t tq = tmem + 2 * D::NT;                 // qp tiles: columns [2NT, 2NT + 64)
     const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-    if (tid == 0)
+    if (tid == 0) {
         for (int t = 0; t < RING && t < ns; ++t) load_stage(t);
+        for (int t = 0; t < QRING && t < ns; ++t) load_qtile(t);
+    }
 
     // q tile (tf32 hi/lo), once per CTA
     if (hf == 0) {
@@ -503,17 +547,18 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     fence_async_smem();
     fence_before();
     __syncthreads();
-    if (tid == 0 && ns > 0) {
-        if (!mbar_wait(&sy->full[0], 0, TC_BUDGET)) set_bad(sy, a.slots);
-        else {
+    // qp of stages 0 and 1; stage t's qp is then issued at stage t-2
+    if (tid == 0) {
+        for (int t = 0; t < 2 && t < ns; ++t) {
+            if (!mbar_wait(&sy->fullq[t], 0, TC_BUDGET)) { set_bad(sy, a.slots); break; }
             fence_after();
-            issue_qp<K>(tq, sAq, sR + 2 * D::B_TILE);
-            commit(&sy->qp_done[0]);
+            issue_qp<K>(tq + t * 32, sAq, sRq + t * GBQ);
+            commit(&sy->qp_done[t]);
         }
     }
 
     for (int s = 0; s < ns; ++s) {
-        const int b = s & 1, bn = b ^ 1, slot = s % RING;
+        const int b = s & 1, slot = s % RING;
         if (!mbar_wait(&sy->full[slot], (s / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         // A buffer b was last read by the MMAs of stage s-2
         if (s >= 2 && !is_bad(sy))
@@ -556,25 +601,23 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         fence_before();
         if (arrive_last(&sy->arrived[b])) {
             fence_after();
-            // the next stage's qp first, so that it does not queue behind this stage's MMAs
-            if (s + 1 < ns) {
-                const int sn = (s + 1) % RING;
-                if (!mbar_wait(&sy->full[sn], ((s + 1) / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+            // qp of stage s+2 into this stage's qp columns (every thread has read
+            // them), ahead of this stage's MMAs
+            if (s + 2 < ns) {
+                const int qs = (s + 2) % QRING;
+                if (!mbar_wait(&sy->fullq[qs], ((s + 2) / QRING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
                 else {
-                    issue_qp<K>(tq + bn * 32, sAq, sR + sn * GB + 2 * D::B_TILE);
-                    commit(&sy->qp_done[bn]);
+                    issue_qp<K>(tq + b * 32, sAq, sRq + qs * GBQ);
+                    commit(&sy->qp_done[b]);
                 }
             }
             const int d = (s / TC_FLUSH) & 1;
-            issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GB, (s % TC_FLUSH) == 0);
+            issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, (s % TC_FLUSH) == 0);
             // mma_done also covers the qp MMA, so that draining it covers every MMA in flight
             commit_stage(sy, s, ns, b);
-            // refill the slot of stage s-1 once its MMAs are done (its qp MMA was
-            // issued before them)
-            if (s >= 1 && s - 1 + RING < ns) {
-                if (!mbar_wait(&sy->mma_done[(s - 1) & 1], ((s - 1) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
-                else load_stage(s - 1 + RING);
-            }
+            refill_ring(sy, a.slots, s, ns, load_stage);
+            // the qp tile slot of stage s is free (its MMA is done: every thread waited for it)
+            if (s + QRING < ns) load_qtile(s + QRING);
         }
         maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
@@ -602,18 +645,21 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
 // stage = 32 individuals.  Thread (jl, ig): block jl, individuals 4ig..4ig+3.
 
 // One (individual, block) pair: qp from q and p (4K values), then U (scaled)
-// and W.
+// and W.  qd[k] = (q_k, q_k); pr2[2k] = (p[k,4j], p[k,4j+1]),
+// pr2[2k+1] = (p[k,4j+2], p[k,4j+3]): the packed FMAs form qp_h for h pairs
+// in the order of the fmaf chain sum_k q_k p[k,m].
 template <int K, bool HESS>
-__device__ __forceinline__ void gen_pair(unsigned nib, const float* qv, const float* pb, float* U4, float* W4,
+__device__ __forceinline__ void gen_pair(unsigned nib, const uint64_t* qd, const uint64_t* pr2, float* U4, float* W4,
                                          const float4* tab) {
-    float qp[4];
+    uint64_t z01 = 0ull, z23 = 0ull;
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
-        float sm = 0.f;
-#pragma unroll
-        for (int k = 0; k < K; ++k) sm = fmaf(qv[k], pb[h * K + k], sm);
-        qp[h] = sm;
+    for (int k = 0; k < K; ++k) {
+        z01 = f2_fma(qd[k], pr2[2 * k], z01);
+        z23 = f2_fma(qd[k], pr2[2 * k + 1], z23);
     }
+    float qp[4];
+    f2_split(z01, qp[0], qp[1]);
+    f2_split(z23, qp[2], qp[3]);
     float L, u[4];
     pair_eval_tab(nib, qp, L, u, tab);
 #pragma unroll
@@ -679,9 +725,13 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
     if (tid == 0)
         for (int t = 0; t < RING && t < ns; ++t) load_stage(t);
 
-    float pr[4 * K];
+    uint64_t pr2[2 * K];
 #pragma unroll
-    for (int t = 0; t < 4 * K; ++t) pr[t] = valid ? (float)a.p[(int64_t)K * 4 * j + t] : 0.25f;
+    for (int k = 0; k < K; ++k) {
+        const double* pj = a.p + (int64_t)K * 4 * j + k;
+        pr2[2 * k] = valid ? f2_pack((float)pj[0], (float)pj[K]) : f2_dup(0.25f);
+        pr2[2 * k + 1] = valid ? f2_pack((float)pj[2 * K], (float)pj[3 * K]) : f2_dup(0.25f);
+    }
     float acc[D::HALF], comp[D::NG];
 #pragma unroll
     for (int c = 0; c < D::HALF; ++c) acc[c] = 0.f;
@@ -703,15 +753,16 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         for (int e = 0; e < 4; ++e) {
             const int ii = ig * 4 + e;
             const unsigned nib = valid ? (Ws[ii] >> bsh) & 0xFu : HX_PAD_NIBBLE;
-            float qv[(K + 3) / 4 * 4];
-            const float4* q4 = reinterpret_cast<const float4*>(Qs + qrow_slot(ii) * QSTR);
+            uint64_t qd[(K + 1) / 2 * 2];
+            const ulonglong2* q2 = reinterpret_cast<const ulonglong2*>(Qs + qrow_slot(ii) * QSTR);
 #pragma unroll
-            for (int c = 0; c < (K + 3) / 4; ++c) {
-                const float4 x = q4[c];
-                qv[4 * c] = x.x; qv[4 * c + 1] = x.y; qv[4 * c + 2] = x.z; qv[4 * c + 3] = x.w;
+            for (int c = 0; c < (K + 1) / 2; ++c) {
+                const ulonglong2 x = q2[c];
+                qd[2 * c] = x.x;
+                qd[2 * c + 1] = x.y;
             }
             float u4[4], w4[4];
-            gen_pair<K, HESS>(nib, qv, pr, u4, w4, s_snp);
+            gen_pair<K, HESS>(nib, qd, pr2, u4, w4, s_snp);
 #pragma unroll
             for (int h = 0; h < 4; ++h) { U[h][e] = u4[h]; if (HESS) W[h][e] = w4[h]; }
         }
@@ -740,10 +791,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
             const int d = (s / TC_FLUSH) & 1;
             issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, sR + slot * GB, (s % TC_FLUSH) == 0);
             commit_stage(sy, s, ns, b);
-            if (s >= 1 && s - 1 + RING < ns) {
-                if (!mbar_wait(&sy->mma_done[(s - 1) & 1], ((s - 1) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
-                else load_stage(s - 1 + RING);
-            }
+            refill_ring(sy, a.slots, s, ns, load_stage);
         }
         maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
@@ -783,7 +831,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
 
 template <int K> constexpr size_t smem_q() {
     using QD = QpDims<K>;
-    return 1024 + 2 * 4 * A_TILE_STD + 2 * QD::A_T + RING * qimg_bytes<K>() + RING * 128 * 4 + sizeof(Sync);
+    return 1024 + 2 * 4 * A_TILE_STD + 2 * QD::A_T + RING * 2 * TcDims<K>::B_TILE + QRING * 2 * QD::B_T +
+           RING * 128 * 4 + sizeof(Sync);
 }
 template <int K> constexpr size_t smem_p() {
     return 1024 + 2 * 4 * A_TILE_PAD + RING * pimg_bytes<K>() + RING * 4 * KD * 4 + sizeof(Sync);
