@@ -14,6 +14,8 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <atomic>
+#include <thread>
 
 using namespace hx;
 
@@ -37,6 +39,9 @@ struct hx_ctx {
     double* h_slots = nullptr;   // pinned
     uint8_t* img = nullptr;      // B-operand image of the tensor-core passes
     int8_t* qp_ws = nullptr;     // P-side QP working sets, warm start of the next solve
+    hx_loop_opts lo{0, 0, 0, -1};  // admixture_qn!/init_em! options
+    double ll_tmp = NAN;         // d.ll_tmp of the step control
+    bool shared_geno = false;    // G and dm belong to the parent context (hx_create_shared)
     int S_q = 1, wpc_q = 1, S_p = 1, ipc_p = 1;
     bool tc = false;                         // Hessian passes on the tensor cores
     int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
@@ -223,42 +228,98 @@ int write_slot(hx_ctx* c, int slot, double v) {
     return HX_OK;
 }
 
-// em! (src/algorithms_inner.jl:29-84): x -> x_next.
+// em! (src/algorithms_inner.jl:29-84): x -> x_next.  With fix_q / fix_p the
+// fixed factor is copied unchanged (the reference rescales a fixed q before
+// projecting it and rebinds p_next to p, :45-52; the intended "keep" is used).
 int em_step(hx_ctx* c) {
-    HX_ST(pass_q(c, qof(c->x), pof(c, c->x), false, c->XtXq, c->Xtzq));
-    HX_ST(pass_p(c, qof(c->x), pof(c, c->x), false, c->XtXp, c->Xtzp));
-    HX_LAUNCH(HX_KIND_OTHER, 1, launch_em_q(qof(c->x), c->Xtzq, c->dm, c->J, c->K, c->I, c->eps, qof(c->xn), c->st));
-    HX_LAUNCH(HX_KIND_OTHER, 1, launch_em_p(pof(c, c->x), c->Xtzp, c->K, c->J, c->eps, pof(c, c->xn), c->st));
+    const size_t nq = (size_t)c->K * c->I * sizeof(double), np = (size_t)c->K * 4 * c->J * sizeof(double);
+    if (!c->lo.fix_q) {
+        HX_ST(pass_q(c, qof(c->x), pof(c, c->x), false, c->XtXq, c->Xtzq));
+        HX_LAUNCH(HX_KIND_OTHER, 1,
+                  launch_em_q(qof(c->x), c->Xtzq, c->dm, c->J, c->K, c->I, c->eps, qof(c->xn), c->st));
+    } else {
+        HX_CK(cudaMemcpyAsync(qof(c->xn), qof(c->x), nq, cudaMemcpyDeviceToDevice, c->st));
+    }
+    if (!c->lo.fix_p) {
+        HX_ST(pass_p(c, qof(c->x), pof(c, c->x), false, c->XtXp, c->Xtzp));
+        HX_LAUNCH(HX_KIND_OTHER, 1, launch_em_p(pof(c, c->x), c->Xtzp, c->K, c->J, c->eps, pof(c, c->xn), c->st));
+    } else {
+        HX_CK(cudaMemcpyAsync(pof(c, c->xn), pof(c, c->x), np, cudaMemcpyDeviceToDevice, c->st));
+    }
     return HX_OK;
 }
 
-// update_q! (src/algorithms_inner.jl:97-211), default (non-penalty) branch.
+// Step control of update_q!/update_p! with guarantee_increase
+// (src/algorithms_inner.jl:169-199, 313-343): x_next = project(x + f d) for
+// f = 1, 1/2, ..., accepted once ll(x_next) >= ll_tmp (Q) or > ll_tmp (P);
+// below f = 1e-3 the loop stops and keeps the last trial.
+template <class STEP>
+int step_control(hx_ctx* c, const double* q_eval, const double* p_eval, bool strict, STEP&& step) {
+    double factor = 1.0;
+    for (;;) {
+        HX_ST(step(factor));
+        HX_ST(loglik_to_slot(c, q_eval, p_eval, S_TMP));
+        HX_ST(read_slots(c));
+        const double ll_new = c->h_slots[S_TMP];
+        if (strict ? ll_new > c->ll_tmp : ll_new >= c->ll_tmp) {
+            c->ll_tmp = ll_new;
+            return HX_OK;
+        }
+        factor /= 2.0;
+        if (factor < 1e-3) factor = 0.0;
+        if (factor == 0.0) return HX_OK;
+    }
+}
+
+// update_q! (src/algorithms_inner.jl:97-211): equality form by default,
+// penalty form (rho 1 1' on each block, no equality) with penalty = 1.
 int update_q(hx_ctx* c, bool update2) {
     double* q = update2 ? qof(c->xn) : qof(c->x);
     double* p = update2 ? pof(c, c->xn) : pof(c, c->x);
     double* out = update2 ? qof(c->xn2) : qof(c->xn);
+    if (c->lo.fix_q) {
+        HX_CK(cudaMemcpyAsync(out, q, (size_t)c->K * c->I * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        return HX_OK;
+    }
     HX_ST(pass_q(c, q, p, true, c->XtXq, c->Xtzq));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_nan_check(c->XtXq, (int64_t)c->K * c->K * c->I, c->slots, c->st));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_nan_check(c->Xtzq, (int64_t)c->K * c->I, c->slots, c->st));
-    HX_LAUNCH(HX_KIND_QP_Q, 1, launch_qp_q(c->K, c->I, c->XtXq, c->Xtzq, q, qof(c->xt), c->slots, c->st));
-    HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_q(q, qof(c->xt), c->K, c->I, c->eps, out, c->st));
-    return HX_OK;
+    HX_LAUNCH(HX_KIND_QP_Q, 1, launch_qp_q(c->K, c->I, c->XtXq, c->Xtzq, q, qof(c->xt), c->slots, c->st,
+                                           c->lo.penalty == 1 ? c->rho : -1.0));
+    auto step = [&](double f) {
+        HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_q(q, qof(c->xt), c->K, c->I, c->eps, out, c->st, f));
+        return HX_OK;
+    };
+    if (!c->lo.guarantee_increase) return step(1.0);
+    return step_control(c, out, p, false, step);
 }
 
-// update_p! (src/algorithms_inner.jl:224-355), default penalty branch.
+// update_p! (src/algorithms_inner.jl:224-355), penalty branch (the default).
 int update_p(hx_ctx* c, bool update2) {
     double* q = update2 ? qof(c->xn2) : qof(c->xn);
     double* p = update2 ? pof(c, c->xn) : pof(c, c->x);
     double* out = update2 ? pof(c, c->xn2) : pof(c, c->xn);
+    if (c->lo.fix_p) {
+        HX_CK(cudaMemcpyAsync(out, p, (size_t)c->K * 4 * c->J * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        return HX_OK;
+    }
     HX_ST(pass_p(c, q, p, true, c->XtXp, c->Xtzp));
     HX_LAUNCH(HX_KIND_QP_P, 1,
               launch_qp_p(c->K, c->J, c->XtXp, c->Xtzp, p, c->rho, pof(c, c->xt), c->slots, c->qp_ws, c->st));
-    HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_p(p, pof(c, c->xt), c->K, c->J, c->eps, out, c->st));
-    return HX_OK;
+    auto step = [&](double f) {
+        HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_p(p, pof(c, c->xt), c->K, c->J, c->eps, out, c->st, f));
+        return HX_OK;
+    };
+    if (!c->lo.guarantee_increase) return step(1.0);
+    return step_control(c, q, out, true, step);
 }
 
 // One outer iteration of admixture_qn! (src/algorithms_outer.jl:65-171).
 int qn_iteration(hx_ctx* c) {
+    if (c->lo.guarantee_increase) {   // d.ll_tmp = d.ll_new (:69-70)
+        HX_ST(read_slots(c));
+        c->ll_tmp = c->h_slots[S_LL_NEW];
+    }
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_iter_begin(c->slots, c->st));
     HX_ST(update_q(c, false));
     HX_ST(update_p(c, false));
@@ -288,13 +349,14 @@ int dalloc(hx_ctx* c, T** p, size_t n) {
 }
 
 int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t nsnp, int64_t I, int64_t J,
-                  int32_t K, const hx_opts* opts, hx_ctx** out) {
+                  int32_t K, const hx_opts* opts, hx_ctx** out, const hx_ctx* parent = nullptr) {
     if (!out) return HX_EINVAL;
     *out = nullptr;
     hx_opts o;
     hx_opts_default(&o);
     if (opts) o = *opts;
-    if (!bed || I <= 0 || J <= 0 || bps < (I + 3) / 4 || nsnp < 2 * J) return HX_EINVAL;
+    if (parent && o.device != parent->device) return HX_EINVAL;
+    if ((!bed && !parent) || I <= 0 || J <= 0 || bps < (I + 3) / 4 || nsnp < 2 * J) return HX_EINVAL;
     if (K < 1 || K > HX_KMAX || o.Qsec < 1 || o.Qsec > HX_QMAX) return HX_EUNSUPPORTED;
     if (o.precision != HX_PREC_FP64 && o.precision != HX_PREC_MIXED) return HX_EINVAL;
     hx_ctx* c = new hx_ctx();
@@ -317,8 +379,14 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_CK(init_tc_attrs());
     plan(c);
     const int NVmax = K + K * (K + 1) / 2;
-    HX_ST(dalloc(c, &c->G, (size_t)c->JW * c->Ipad));
-    HX_ST(dalloc(c, &c->dm, (size_t)I));
+    if (parent) {
+        c->G = parent->G;
+        c->dm = parent->dm;
+        c->shared_geno = true;
+    } else {
+        HX_ST(dalloc(c, &c->G, (size_t)c->JW * c->Ipad));
+        HX_ST(dalloc(c, &c->dm, (size_t)I));
+    }
     for (double** b : {&c->x, &c->xn, &c->xn2, &c->xt, &c->xio}) HX_ST(dalloc(c, b, (size_t)c->nx));
     HX_ST(dalloc(c, &c->U, (size_t)c->nx * c->Qs));
     HX_ST(dalloc(c, &c->V, (size_t)c->nx * c->Qs));
@@ -339,10 +407,14 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_CK(cudaMallocHost((void**)&c->h_slots, HX_NSLOT * sizeof(double)));
     HX_CK(cudaMemsetAsync(c->U, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
     HX_CK(cudaMemsetAsync(c->V, 0, (size_t)c->nx * c->Qs * sizeof(double), c->st));
-    HX_CK(cudaMemsetAsync(c->dm, 0, (size_t)I * sizeof(unsigned long long), c->st));
     for (int s = 0; s < HX_NSLOT; ++s) c->h_slots[s] = 0.0;
     c->h_slots[S_LL_NEW] = NAN;
     HX_CK(cudaMemcpyAsync(c->slots, c->h_slots, HX_NSLOT * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    if (parent) {
+        HX_CK(cudaStreamSynchronize(c->st));
+        return HX_OK;
+    }
+    HX_CK(cudaMemsetAsync(c->dm, 0, (size_t)I * sizeof(unsigned long long), c->st));
     // stage the BED matrix (first 2J SNPs used by the fit; all n_snp SNPs for
     // the double-missing count, as count_double_missing! reads the whole file)
     const uint8_t* dbed = bed;
@@ -397,6 +469,24 @@ struct Tmp {  // temporary device buffers of the host-array entry points
 // ====================================================================== C ABI
 extern "C" {
 
+int hx_loop_opts_default(hx_loop_opts* o) {
+    if (!o) return HX_EINVAL;
+    o->fix_q = 0;
+    o->fix_p = 0;
+    o->guarantee_increase = 0;
+    o->penalty = -1;
+    return HX_OK;
+}
+
+int hx_set_loop_opts(hx_ctx* c, const hx_loop_opts* o) {
+    if (!c || !o) return HX_EINVAL;
+    if (o->penalty == 0)
+        return fail(c, HX_EUNSUPPORTED, "penalty = 0 (P-step equality form, algorithms_inner.jl:306-310) is not built");
+    if (o->penalty != -1 && o->penalty != 1) return fail(c, HX_EINVAL, "penalty must be -1, 0 or 1");
+    c->lo = *o;
+    return HX_OK;
+}
+
 int hx_opts_default(hx_opts* o) {
     if (!o) return HX_EINVAL;
     o->precision = HX_PREC_FP64;
@@ -438,7 +528,7 @@ int hx_create_device(const uint8_t* d_bed, int64_t bps, int64_t nsnp, int64_t I,
 int hx_destroy(hx_ctx* c) {
     if (!c) return HX_OK;
     if (c->st) cudaStreamSynchronize(c->st);
-    void* bufs[] = {c->G, c->dm, c->x, c->xn, c->xn2, c->xt, c->xio, c->U, c->V, c->XtXq, c->Xtzq, c->XtXp,
+    void* bufs[] = {c->shared_geno ? nullptr : (void*)c->G, c->shared_geno ? nullptr : (void*)c->dm, c->x, c->xn, c->xn2, c->xt, c->xio, c->U, c->V, c->XtXq, c->Xtzq, c->XtXp,
                     c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots, c->img, c->qp_ws};
     for (void* b : bufs) if (b) cudaFree(b);
     prof_resolve(c);
@@ -771,6 +861,40 @@ int hx_admixture_qn(hx_ctx* c, int32_t n_iter, double rtol, int32_t iter_offset,
         info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return HX_OK;
+}
+
+int hx_create_shared(const hx_ctx* parent, int32_t K, const hx_opts* opts, hx_ctx** out) {
+    if (!parent || !out) return HX_EINVAL;
+    hx_opts o;
+    hx_opts_default(&o);
+    if (opts) o = *opts;
+    o.device = parent->device;
+    return create_common(nullptr, true, parent->bps, parent->nsnp, parent->I, parent->J, K, &o, out, parent);
+}
+
+int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int32_t em_iters, int32_t threads,
+                hx_fit_info* infos, int32_t* status) {
+    if (!ctxs || n < 0 || !infos) return HX_EINVAL;
+    for (int32_t a = 0; a < n; ++a)
+        if (!ctxs[a]) return HX_EINVAL;
+    const int nt = std::max(1, std::min<int>(threads > 0 ? threads : n, n));
+    std::atomic<int> next(0);
+    std::vector<int> st(n, HX_OK);
+    auto worker = [&]() {
+        for (int a = next++; a < n; a = next++) {
+            if (cudaSetDevice(ctxs[a]->device) != cudaSuccess) { st[a] = HX_ECUDA; continue; }
+            st[a] = hx_fit(ctxs[a], n_iter, rtol, em_iters, &infos[a]);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+    int first = HX_OK;
+    for (int32_t a = 0; a < n; ++a) {
+        if (status) status[a] = st[a];
+        if (first == HX_OK && st[a] != HX_OK) first = st[a];
+    }
+    return first;
 }
 
 int hx_fit(hx_ctx* c, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_info* info) {

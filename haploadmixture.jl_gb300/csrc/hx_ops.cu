@@ -215,17 +215,17 @@ __global__ void k_em_p(const double* __restrict__ p, const double* __restrict__ 
 }
 
 __global__ void k_step_q(const double* __restrict__ q, const double* __restrict__ d, int K, int64_t ncol, double eps,
-                         double* __restrict__ out) {
+                         double* __restrict__ out, double factor) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ncol) return;
     double v[HX_KMAX];
-    for (int k = 0; k < K; ++k) v[k] = q[(int64_t)K * i + k] + (d ? d[(int64_t)K * i + k] : 0.0);
+    for (int k = 0; k < K; ++k) v[k] = q[(int64_t)K * i + k] + (d ? factor * d[(int64_t)K * i + k] : 0.0);
     project_simplex(v, K, eps);
     for (int k = 0; k < K; ++k) out[(int64_t)K * i + k] = v[k];
 }
 
 __global__ void k_step_p(const double* __restrict__ p, const double* __restrict__ d, int K, int64_t J, double eps,
-                         double* __restrict__ out) {
+                         double* __restrict__ out, double factor) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)K * J) return;
     const int64_t j = t / K;
@@ -233,7 +233,7 @@ __global__ void k_step_p(const double* __restrict__ p, const double* __restrict_
     double v[4];
     for (int h = 0; h < 4; ++h) {
         const int64_t a = (int64_t)K * (4 * j + h) + k;
-        v[h] = p[a] + (d ? d[a] : 0.0);
+        v[h] = p[a] + (d ? factor * d[a] : 0.0);
     }
     project_simplex(v, 4, eps);
     for (int h = 0; h < 4; ++h) out[(int64_t)K * (4 * j + h) + k] = v[h];
@@ -445,7 +445,8 @@ __host__ __device__ constexpr size_t qp_warp_bytes(int nmax) {
 struct HQ {
     const double* X;
     int K;
-    __device__ double operator()(int r, int c) const { return X[r + K * c]; }
+    double pen;   // penalty form: rho on every entry (rho * 1 1'); 0 in the equality form
+    __device__ double operator()(int r, int c) const { return X[r + K * c] + pen; }
 };
 struct HP {
     const double* X;   // XtX_p + K*K*4j
@@ -459,7 +460,7 @@ struct HP {
 
 __global__ void __launch_bounds__(32 * QP_WARPS)
 k_qp_q(int K, int64_t n, const double* __restrict__ XtX, const double* __restrict__ Xtz,
-       const double* __restrict__ q, double* __restrict__ qdiff, double* slots) {
+       const double* __restrict__ q, double* __restrict__ qdiff, double* slots, double pen_rho) {
     extern __shared__ double smem_qp[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t pidx = (int64_t)blockIdx.x * QP_WARPS + warp;
@@ -474,8 +475,8 @@ k_qp_q(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
         w.st[a] = (w.lo[a] >= 0.0 && w.hi[a] <= 0.0) ? QL : QF;
     }
     __syncwarp();
-    HQ H{XtX + (int64_t)K * K * pidx, K};
-    const int it = warp_qp(K, true, H, w);
+    HQ H{XtX + (int64_t)K * K * pidx, K, pen_rho >= 0.0 ? pen_rho : 0.0};
+    const int it = warp_qp(K, pen_rho < 0.0, H, w);
     __syncwarp();
     for (int a = lane; a < K; a += 32) qdiff[(int64_t)K * pidx + a] = w.d[a];
     if (it < 0 && lane == 0) atomicAdd(slots + S_QP_FAIL, 1.0);
@@ -705,13 +706,13 @@ cudaError_t launch_em_p(const double* p, const double* Xtz, int K, int64_t J, do
     return cudaGetLastError();
 }
 cudaError_t launch_step_q(const double* q, const double* d, int K, int64_t ncol, double eps, double* out,
-                          cudaStream_t st) {
-    k_step_q<<<nblk(ncol, 128), 128, 0, st>>>(q, d, K, ncol, eps, out);
+                          cudaStream_t st, double factor) {
+    k_step_q<<<nblk(ncol, 128), 128, 0, st>>>(q, d, K, ncol, eps, out, factor);
     return cudaGetLastError();
 }
 cudaError_t launch_step_p(const double* p, const double* d, int K, int64_t J, double eps, double* out,
-                          cudaStream_t st) {
-    k_step_p<<<nblk((int64_t)K * J, 128), 128, 0, st>>>(p, d, K, J, eps, out);
+                          cudaStream_t st, double factor) {
+    k_step_p<<<nblk((int64_t)K * J, 128), 128, 0, st>>>(p, d, K, J, eps, out, factor);
     return cudaGetLastError();
 }
 cudaError_t init_kernel_attrs() {
@@ -719,9 +720,9 @@ cudaError_t init_kernel_attrs() {
                                 (int)(QP_WARPS * qp_warp_bytes(4 * HX_KMAX)));
 }
 cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff,
-                        double* slots, cudaStream_t st) {
+                        double* slots, cudaStream_t st, double pen_rho) {
     const size_t smem = QP_WARPS * qp_warp_bytes(K);
-    k_qp_q<<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, q, qdiff, slots);
+    k_qp_q<<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, q, qdiff, slots, pen_rho);
     return cudaGetLastError();
 }
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,

@@ -66,13 +66,13 @@ cudaError_t launch_em_p(const double* p, const double* Xtz, int K, int64_t J, do
                         cudaStream_t st);
 // q_next = project(q + d) per column / quartet; d may be null (plain projection)
 cudaError_t launch_step_q(const double* q, const double* d, int K, int64_t ncol, double eps, double* out,
-                          cudaStream_t st);
+                          cudaStream_t st, double factor = 1.0);
 cudaError_t launch_step_p(const double* p, const double* d, int K, int64_t J, double eps, double* out,
-                          cudaStream_t st);
+                          cudaStream_t st, double factor = 1.0);
 // batched QP (init_kernel_attrs: once per device, before the first launch)
 cudaError_t init_kernel_attrs();
 cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff,
-                        double* slots, cudaStream_t st);
+                        double* slots, cudaStream_t st, double pen_rho = -1.0);
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
                         double* pdiff, double* slots, int8_t* ws, cudaStream_t st);
 // ZAL quasi-Newton

@@ -25,6 +25,11 @@ class HxOpts(C.Structure):
                 ("rho", C.c_double), ("pseudocount", C.c_double), ("path", C.c_int32), ("reserved", C.c_int32)]
 
 
+class HxLoopOpts(C.Structure):
+    _fields_ = [("fix_q", C.c_int32), ("fix_p", C.c_int32), ("guarantee_increase", C.c_int32),
+                ("penalty", C.c_int32)]
+
+
 class HxIterInfo(C.Structure):
     _fields_ = [("iter", C.c_int32), ("accepted_qn", C.c_int32), ("ll_prev", C.c_double),
                 ("ll_basic", C.c_double), ("ll_qn", C.c_double), ("ll_new", C.c_double),
@@ -44,6 +49,10 @@ I32 = C.c_int32
 # name -> (restype, argtypes); every entry point of include/haplo_gb300.h
 SIGNATURES = {
     "hx_opts_default": (I32, [C.POINTER(HxOpts)]),
+    "hx_loop_opts_default": (I32, [C.POINTER(HxLoopOpts)]),
+    "hx_create_shared": (I32, [P, I32, C.POINTER(HxOpts), C.POINTER(P)]),
+    "hx_fit_many": (I32, [C.POINTER(P), I32, I32, C.c_double, I32, I32, C.POINTER(HxFitInfo), C.POINTER(I32)]),
+    "hx_set_loop_opts": (I32, [P, C.POINTER(HxLoopOpts)]),
     "hx_status_string": (C.c_char_p, [I32]),
     "hx_last_error": (C.c_char_p, [P]),
     "hx_create": (I32, [P, I64, I64, I64, I64, I32, C.POINTER(HxOpts), C.POINTER(P)]),

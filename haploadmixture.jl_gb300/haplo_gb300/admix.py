@@ -75,6 +75,35 @@ class GB300Admix:
             raise _lib.HxError(st, msg)
         self.bytes_per_snp, self.n_snp = bytes_per_snp, n_snp
 
+    @classmethod
+    def shared(cls, parent, K, *, precision=None, Q=3, rho=1e7, pseudocount=1e-5, path="auto"):
+        """A context for K ancestries on the parent's decoded genotypes
+        (hx_create_shared); it keeps the parent alive."""
+        lib = _lib.load()
+        self = cls.__new__(cls)
+        self.I, self.J, self.K = parent.I, parent.J, int(K)
+        self.precision = precision or parent.precision
+        self.Q = Q
+        opts = _lib.HxOpts()
+        lib.hx_opts_default(C.byref(opts))
+        opts.precision = {"fp64": _lib.HX_PREC_FP64, "mixed": _lib.HX_PREC_MIXED}[self.precision]
+        opts.Qsec = Q
+        opts.rho = rho
+        opts.pseudocount = pseudocount
+        opts.path = {"auto": _lib.HX_PATH_AUTO, "cuda_cores": _lib.HX_PATH_CUDA_CORES}[path]
+        h = C.c_void_p()
+        st = lib.hx_create_shared(parent._h, self.K, C.byref(opts), C.byref(h))
+        self._h = h
+        self._parent = parent
+        if st != _lib.HX_OK:
+            msg = lib.hx_last_error(h).decode() if h.value else ""
+            if h.value:
+                lib.hx_destroy(h)
+            self._h = None
+            raise _lib.HxError(st, msg)
+        self.bytes_per_snp, self.n_snp = parent.bytes_per_snp, parent.n_snp
+        return self
+
     # -- lifetime
     def close(self):
         if getattr(self, "_h", None):
@@ -142,6 +171,15 @@ class GB300Admix:
 
     # -- launch accounting
     KINDS = ("accum_q", "accum_p", "loglik", "qp_q", "qp_p", "qn", "other")
+
+    def set_loop_opts(self, fix_q=False, fix_p=False, guarantee_increase=False, penalty=None):
+        """admixture_qn!/init_em! keyword options (src/algorithms_outer.jl:1-3, 38-41);
+        penalty None is the reference default, True the penalty form for both steps."""
+        o = _lib.HxLoopOpts()
+        self._ck(self.lib.hx_loop_opts_default(C.byref(o)))
+        o.fix_q, o.fix_p, o.guarantee_increase = int(fix_q), int(fix_p), int(guarantee_increase)
+        o.penalty = -1 if penalty is None else int(bool(penalty))
+        self._ck(self.lib.hx_set_loop_opts(self._h, C.byref(o)))
 
     def set_profiling(self, on=True):
         self._ck(self.lib.hx_set_profiling(self._h, 1 if on else 0))

@@ -77,8 +77,25 @@ typedef struct hx_fit_info {
     double seconds;        /* wall time of the call */
 } hx_fit_info;
 
+/* Loop options of admixture_qn! / init_em! (src/algorithms_outer.jl:1-3,
+ * 38-41; src/driver.jl:54-55).  Set per context with hx_set_loop_opts; they
+ * apply to hx_init_em, hx_update_q/p, hx_qn_iteration, hx_admixture_qn and
+ * hx_fit. */
+typedef struct hx_loop_opts {
+    int32_t fix_q;               /* 1: Q stays unchanged (q_next = q) */
+    int32_t fix_p;               /* 1: P stays unchanged */
+    int32_t guarantee_increase;  /* 1: halve each update's step until the log-likelihood does not drop
+                                    (src/algorithms_inner.jl:169-199 Q with >=, :313-343 P with >) */
+    int32_t penalty;             /* -1 (default, penalty=nothing): P penalty form, Q equality form;
+                                    1: penalty form for both (rho * 1 1' on each Q block);
+                                    0: equality forms for both -> HX_EUNSUPPORTED (P equality form not built) */
+} hx_loop_opts;
+
 /* Defaults: precision FP64, device 0, Qsec 3, rho 1e7, pseudocount 1e-5. */
 int hx_opts_default(hx_opts* opts);
+/* Defaults: no fixed factor, no step control, penalty -1. */
+int hx_loop_opts_default(hx_loop_opts* opts);
+int hx_set_loop_opts(hx_ctx* ctx, const hx_loop_opts* opts);
 const char* hx_status_string(int status);
 const char* hx_last_error(const hx_ctx* ctx);
 
@@ -148,6 +165,25 @@ int hx_admixture_qn(hx_ctx* ctx, int32_t n_iter, double rtol, int32_t iter_offse
 /* _admixture_base's fit sequence (driver.jl:181-197): init_em! (em_iters) then
  * admixture_qn!.  Starts from the current x. */
 int hx_fit(hx_ctx* ctx, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_info* info);
+
+/* Batched fits for the K sweep with random restarts (README.md:9 names AIC
+ * model selection; run_admixture fits one K per call, src/driver.jl:38-79).
+ * No reference counterpart: the reference runs such sweeps as separate
+ * run_admixture calls.
+ *
+ * hx_create_shared: a context for K ancestries that shares the parent's
+ * decoded genotype classes and double-missing counts (no second upload or
+ * decode).  The parent must outlive it.  opts->device is ignored (the
+ * parent's device is used).
+ *
+ * hx_fit_many: hx_fit on each of n contexts, up to `threads` at a time (0 =
+ * all) from host threads, each context on its own CUDA stream, so that the
+ * fits' kernels overlap on the GPU.  Each context gives the same result as
+ * hx_fit alone.  status (optional, n entries) receives each fit's status;
+ * the return value is the first non-OK status, or HX_OK. */
+int hx_create_shared(const hx_ctx* parent, int32_t K, const hx_opts* opts, hx_ctx** out);
+int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int32_t em_iters, int32_t threads,
+                hx_fit_info* infos, int32_t* status);
 
 /* ---- launch accounting (no counterpart in the reference, which prints
  * @time per phase, src/algorithms_inner.jl:114,135,241,259) ---- */

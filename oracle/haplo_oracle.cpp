@@ -491,16 +491,25 @@ void project_p_all(double* p, int K, int64_t J, double eps, int nthreads) {
 
 // src/algorithms_inner.jl:134-168 (non-penalty branch) for every individual.
 // Xtz is the gradient as accumulated (before the reference's `Xtz .*= -1`).
+// pen_rho < 0: the default equality form (sum d = 0, src/algorithms_inner.jl:
+// 163-166).  pen_rho >= 0: the penalty form of :158-162, H + rho 1 1' and no
+// equality (the reference adds rho to the whole XtX array inside the loop over
+// i, algorithms_inner.jl:159; the intended per-individual penalty is used).
 int qp_q_batch(int K, int64_t I, const double* XtX, const double* Xtz, const double* q, double* qdiff,
-               int nthreads) {
+               int nthreads, double pen_rho = -1.0) {
     std::atomic<int> fails(0);
     parallel_for(I, nthreads, [&](int64_t a, int64_t b) {
-        std::vector<double> lo(K), hi(K);
+        std::vector<double> lo(K), hi(K), H((size_t)K * K);
         for (int64_t i = a; i < b; ++i) {
             const double* qi = q + (int64_t)K * i;
             for (int k = 0; k < K; ++k) { lo[k] = 0.0 - qi[k]; hi[k] = 1.0 - qi[k]; }
-            int it = qp_active_set(K, XtX + (int64_t)K * K * i, Xtz + (int64_t)K * i, lo.data(), hi.data(),
-                                   true, qdiff + (int64_t)K * i);
+            const double* Hi = XtX + (int64_t)K * K * i;
+            if (pen_rho >= 0.0) {
+                for (int e = 0; e < K * K; ++e) H[e] = Hi[e] + pen_rho;
+                Hi = H.data();
+            }
+            int it = qp_active_set(K, Hi, Xtz + (int64_t)K * i, lo.data(), hi.data(), pen_rho < 0.0,
+                                   qdiff + (int64_t)K * i);
             if (it < 0) fails++;
         }
     });
@@ -718,13 +727,73 @@ void orc_zal(int64_t n, const double* x, const double* x_next, const double* x_n
     }
 }
 
+// Loop options of admixture_qn!/init_em! (src/algorithms_outer.jl:1-3, 38-41):
+// fix_q / fix_p keep Q or P; guarantee_increase halves each update's step
+// until the log-likelihood does not drop (src/algorithms_inner.jl:169-199 for
+// Q with >=, :313-343 for P with >); penalty -1 is the default (P penalty
+// form, Q equality form), 1 the penalty form for both.  The P equality form
+// (penalty 0) is not restated.
+struct LoopOpts {
+    int fix_q = 0, fix_p = 0, gi = 0, penalty = -1;
+};
+
+namespace {
+// update_q! with the loop options; ll_tmp is d.ll_tmp.
+void update_q_opts(const Dims& D, const double* q, const double* p, double* q_next, const LoopOpts& o, double rho,
+                   double& ll_tmp, int nthreads) {
+    const int K = D.K;
+    const int64_t n = (int64_t)K * D.I;
+    if (o.fix_q) { std::memcpy(q_next, q, n * sizeof(double)); return; }
+    std::vector<double> XtX((size_t)K * K * D.I), Xtz((size_t)n), qd((size_t)n);
+    accum_q(D, q, p, XtX.data(), Xtz.data(), nthreads);
+    qp_q_batch(K, D.I, XtX.data(), Xtz.data(), q, qd.data(), nthreads, o.penalty == 1 ? rho : -1.0);
+    double factor = 1.0;
+    for (;;) {
+        for (int64_t a = 0; a < n; ++a) q_next[a] = q[a] + factor * qd[a];
+        project_q_all(q_next, K, D.I, 1e-5, nthreads);
+        if (!o.gi) break;
+        const double ll_new = loglik(D, q_next, p, 2, nthreads);
+        if (ll_new >= ll_tmp) { ll_tmp = ll_new; break; }
+        factor /= 2.0;
+        if (factor < 1e-3) factor = 0.0;
+        if (factor == 0.0) break;
+    }
+}
+void update_p_opts(const Dims& D, const double* q, const double* p, double* p_next, const LoopOpts& o, double rho,
+                   double& ll_tmp, int nthreads) {
+    const int K = D.K;
+    const int64_t n = (int64_t)K * 4 * D.J;
+    if (o.fix_p) { std::memcpy(p_next, p, n * sizeof(double)); return; }
+    std::vector<double> XtX((size_t)K * K * 4 * D.J), Xtz((size_t)n), pd((size_t)n);
+    accum_p(D, q, p, XtX.data(), Xtz.data(), nthreads);
+    qp_p_batch(K, D.J, XtX.data(), Xtz.data(), p, rho, pd.data(), nthreads);
+    double factor = 1.0;
+    for (;;) {
+        for (int64_t a = 0; a < n; ++a) p_next[a] = p[a] + factor * pd[a];
+        project_p_all(p_next, K, D.J, 1e-5, nthreads);
+        if (!o.gi) break;
+        const double ll_new = loglik(D, q, p_next, 2, nthreads);
+        if (ll_new > ll_tmp) { ll_tmp = ll_new; break; }
+        factor /= 2.0;
+        if (factor < 1e-3) factor = 0.0;
+        if (factor == 0.0) break;
+    }
+}
+}  // namespace
+
 // src/algorithms_outer.jl:1-22 (init_em!) followed by :38-172 (admixture_qn!,
-// mode = :ZAL, penalty = nothing -> p_penalty, no q_penalty).
-// x (K x (I+4J)) holds the initial [q | p] and receives the final one.
-// trace (optional, n_iter entries) receives ll after every outer iteration.
-int orc_fit(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J, int K, int Qs, double* x,
-            int n_iter, double rtol, int em_iters, double rho, int nthreads, double* ll_out, int* iters_out,
-            double* trace) {
+// mode = :ZAL) with the loop options above.  x (K x (I+4J)) holds the initial
+// [q | p] and receives the final one; trace (optional, n_iter entries)
+// receives ll after every outer iteration.  EM with fix_q / fix_p keeps that
+// factor unchanged (the reference's em! rescales a fixed q before projecting
+// it and rebinds p_next to p, algorithms_inner.jl:45-52, which is not
+// restated).  Returns 0, or -2 for the unsupported P equality form.
+int orc_fit_ex(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J, int K, int Qs, double* x,
+               int n_iter, double rtol, int em_iters, double rho, int nthreads, double* ll_out, int* iters_out,
+               double* trace, int fix_q, int fix_p, int guarantee_increase, int penalty) {
+    LoopOpts o;
+    o.fix_q = fix_q; o.fix_p = fix_p; o.gi = guarantee_increase; o.penalty = penalty;
+    if (penalty == 0) return -2;
     Dims D{bed, bps, nsnp, I, J, K};
     const int64_t n = (int64_t)K * (I + 4 * J);
     std::vector<int64_t> dm(I);
@@ -735,6 +804,8 @@ int orc_fit(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J,
     double ll_new = NAN;
     for (int e = 0; e < em_iters; ++e) {
         orc_em_step(bed, bps, I, J, K, dm.data(), q, p, xn.data(), xn.data() + (int64_t)K * I, nthreads);
+        if (o.fix_q) std::memcpy(xn.data(), q, (size_t)K * I * sizeof(double));
+        if (o.fix_p) std::memcpy(xn.data() + (int64_t)K * I, p, (size_t)K * 4 * J * sizeof(double));
         std::memcpy(x, xn.data(), n * sizeof(double));
         ll_new = loglik(D, q, p, 2, nthreads);
         project_p_all(p, K, J, 1e-5, nthreads);
@@ -744,14 +815,15 @@ int orc_fit(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J,
     int it = 0;
     for (it = 1; it <= n_iter; ++it) {
         double ll_prev = ll_new;
+        double ll_tmp = ll_new;
         double* qn = xn.data();
         double* pn = xn.data() + (int64_t)K * I;
         double* qn2 = xn2.data();
         double* pn2 = xn2.data() + (int64_t)K * I;
-        orc_update_q(bed, bps, I, J, K, q, p, qn, nullptr, nullptr, nthreads);
-        orc_update_p(bed, bps, I, J, K, qn, p, rho, pn, nullptr, nullptr, nthreads);
-        orc_update_q(bed, bps, I, J, K, qn, pn, qn2, nullptr, nullptr, nthreads);
-        orc_update_p(bed, bps, I, J, K, qn2, pn, rho, pn2, nullptr, nullptr, nthreads);
+        update_q_opts(D, q, p, qn, o, rho, ll_tmp, nthreads);
+        update_p_opts(D, qn, p, pn, o, rho, ll_tmp, nthreads);
+        update_q_opts(D, qn, pn, qn2, o, rho, ll_tmp, nthreads);
+        update_p_opts(D, qn2, pn, pn2, o, rho, ll_tmp, nthreads);
         double ll_basic = loglik(D, qn2, pn2, 2, nthreads);
         orc_zal(n, x, xn.data(), xn2.data(), U.data(), V.data(), Qs, it, xt.data());
         project_p_all(xt.data() + (int64_t)K * I, K, J, 1e-5, nthreads);
@@ -771,6 +843,14 @@ int orc_fit(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J,
     if (ll_out) *ll_out = ll_new;
     if (iters_out) *iters_out = it > n_iter ? n_iter : it;
     return 0;
+}
+
+// The default options (src/driver.jl:38-58 defaults).
+int orc_fit(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J, int K, int Qs, double* x,
+            int n_iter, double rtol, int em_iters, double rho, int nthreads, double* ll_out, int* iters_out,
+            double* trace) {
+    return orc_fit_ex(bed, bps, nsnp, I, J, K, Qs, x, n_iter, rtol, em_iters, rho, nthreads, ll_out, iters_out,
+                      trace, 0, 0, 0, -1);
 }
 
 // ---------------------------------------------------------------- synthetic

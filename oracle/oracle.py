@@ -50,6 +50,8 @@ def _load():
             "orc_update_p": (I32, [P, I64, I64, I64, I32, P, P, Dd, P, P, P, I32]),
             "orc_zal": (None, [I64, P, P, P, P, P, I32, I32, P]),
             "orc_fit": (I32, [P, I64, I64, I64, I64, I32, I32, P, I32, Dd, I32, Dd, I32, P, P, P]),
+            "orc_fit_ex": (I32, [P, I64, I64, I64, I64, I32, I32, P, I32, Dd, I32, Dd, I32, P, P, P,
+                                 I32, I32, I32, I32]),
             "orc_synth": (None, [C.c_uint64, I64, I64, I32, P, P, Dd, P, I32]),
         }
         for name, (res, args) in sig.items():
@@ -208,15 +210,22 @@ def zal(x, x_next, x_next2, U, V, it):
     return xt, U, V
 
 
-def fit(b, K, q, p, n_iter=1000, rtol=1e-7, em_iters=5, Qs=3, rho=1e7, threads=None):
-    """init_em! + admixture_qn! on the CPU; returns (q, p, ll, iters, trace)."""
+def fit(b, K, q, p, n_iter=1000, rtol=1e-7, em_iters=5, Qs=3, rho=1e7, threads=None, fix_q=False, fix_p=False,
+        guarantee_increase=False, penalty=None):
+    """init_em! + admixture_qn! on the CPU; returns (q, p, ll, iters, trace).
+    penalty None is the reference default (P penalty form, Q equality form);
+    True uses the penalty form for both."""
     q, p = _F(q, (K, b.I)), _F(p, (K, 4 * b.J))
     x = np.asfortranarray(np.hstack([q, p]))
     ll = C.c_double()
     iters = C.c_int32()
     trace = np.full(n_iter, np.nan)
-    _load().orc_fit(b.ptr, b.bps, b.n_snp, b.I, b.J, K, Qs, _p(x), n_iter, rtol, em_iters, rho,
-                    threads or nthreads(), C.byref(ll), C.byref(iters), _p(trace))
+    pen = -1 if penalty is None else int(bool(penalty))
+    r = _load().orc_fit_ex(b.ptr, b.bps, b.n_snp, b.I, b.J, K, Qs, _p(x), n_iter, rtol, em_iters, rho,
+                           threads or nthreads(), C.byref(ll), C.byref(iters), _p(trace), int(fix_q), int(fix_p),
+                           int(guarantee_increase), pen)
+    if r == -2:
+        raise NotImplementedError("the P equality form (penalty=False) is not restated")
     return (np.asfortranarray(x[:, :b.I]), np.asfortranarray(x[:, b.I:]), ll.value, iters.value,
             trace[:iters.value])
 

@@ -193,3 +193,33 @@ def test_errors_are_status_codes(hx, coh):
     d = make(hx, coh)
     with pytest.raises(HxError):
         d.update_q()                                               # Q/P not set yet
+
+
+@pytest.mark.parametrize("opts", [dict(fix_q=True), dict(fix_p=True), dict(guarantee_increase=True),
+                                  dict(penalty=True)])
+def test_loop_options_match_oracle_fp64(hx, O, opts):
+    # admixture_qn!/init_em! keywords (src/algorithms_outer.jl:1-3, 38-41)
+    c = small_cohort(240, 120, 3, seed=33, alpha=0.5, miss=0.01)
+    b = O.Bed(c["bed"], c["I"], c["J"])
+    q0, p0 = start(c, seed=5)
+    q0, p0 = O.project_q(q0), O.project_p(p0)
+    qo, po, llo, ito, _ = O.fit(b, 3, q0, p0, n_iter=60, rtol=1e-8, em_iters=2, **opts)
+    d = make(hx, c)
+    d.set_loop_opts(**opts)
+    d.set_qp(q0, p0)
+    info = d.fit(n_iter=60, rtol=1e-8, em_iters=2)
+    qd, pd = d.get_qp()
+    assert info["ll"] == pytest.approx(llo, rel=1e-9)
+    assert abs(info["iters"] - ito) <= 1
+    assert np.abs(qd - qo).max() < 1e-6 and np.abs(pd - po).max() < 1e-6
+    if opts.get("fix_q"):
+        np.testing.assert_allclose(qd, q0, rtol=0, atol=1e-15)
+    if opts.get("fix_p"):
+        np.testing.assert_allclose(pd, p0, rtol=0, atol=1e-15)
+
+
+def test_p_equality_form_is_reported_unsupported(hx, coh):
+    from haplo_gb300 import HxError
+    d = make(hx, coh)
+    with pytest.raises(HxError):
+        d.set_loop_opts(penalty=False)

@@ -213,3 +213,62 @@ def test_fit_beats_truth_and_converges(O):
     assert ll >= O.loglik(b, 3, c["Q"], c["P"])
     assert trace[-1] > trace[0]
     assert ll == pytest.approx(O.loglik(b, 3, q, p), rel=1e-12)
+
+
+# ---- loop options of admixture_qn!/init_em! (src/algorithms_outer.jl:1-3, 38-41)
+
+@pytest.fixture(scope="module")
+def loop_case(O):
+    c = small_cohort(240, 120, 3, seed=33, alpha=0.5, miss=0.01)
+    b = O.Bed(c["bed"], c["I"], c["J"])
+    from haplo_gb300.admix import random_init
+    q0, p0 = random_init(c["I"], c["J"], 3, np.random.default_rng(5))
+    # start on the feasible set, which init_em!'s projections leave in place
+    return c, b, O.project_q(q0), O.project_p(p0)
+
+
+def test_fix_q_and_fix_p_keep_that_factor(O, loop_case):
+    c, b, q0, p0 = loop_case
+    q, p, ll, it, _ = O.fit(b, 3, q0, p0, n_iter=20, rtol=1e-9, em_iters=2, fix_q=True)
+    np.testing.assert_allclose(q, q0, rtol=0, atol=1e-15)
+    assert not np.allclose(p, p0)
+    assert ll > O.loglik(b, 3, q0, p0)
+    q, p, ll, it, _ = O.fit(b, 3, q0, p0, n_iter=20, rtol=1e-9, em_iters=2, fix_p=True)
+    np.testing.assert_allclose(p, p0, rtol=0, atol=1e-15)
+    assert not np.allclose(q, q0)
+
+
+def test_guarantee_increase_never_lowers_the_loglik(O, loop_case):
+    c, b, q0, p0 = loop_case
+    q, p, ll, it, trace = O.fit(b, 3, q0, p0, n_iter=40, rtol=1e-10, em_iters=0, guarantee_increase=True)
+    assert np.all(np.diff(trace) >= -1e-9 * np.abs(trace[1:]))
+    _, _, ll_plain, _, _ = O.fit(b, 3, q0, p0, n_iter=300, rtol=1e-10, em_iters=0)
+    assert ll == pytest.approx(ll_plain, rel=1e-4)
+
+
+def test_q_penalty_form_solves_the_penalised_qp(O, coh):
+    # penalty = true: min 0.5 d'(H + rho 1 1')d - z'd over the box, no equality
+    b = O.Bed(coh["bed"], coh["I"], coh["J"])
+    K = coh["K"]
+    from haplo_gb300.admix import random_init
+    q, p = random_init(coh["I"], coh["J"], K, np.random.default_rng(2))
+    XtX, Xtz = O.accum_q(b, K, q, p)
+    rho = 1e7
+    for i in range(0, coh["I"], 37):
+        H = XtX[:, :, i] + rho
+        d, it = O.qp_dense(H, Xtz[:, i], -q[:, i], 1 - q[:, i], False)
+        assert it > 0
+        g = H @ d - Xtz[:, i]
+        lo, hi = -q[:, i], 1 - q[:, i]
+        free = (d > lo + 1e-12) & (d < hi - 1e-12)
+        assert np.all(np.abs(g[free]) <= 1e-6 * max(1.0, np.abs(Xtz[:, i]).max()))
+        assert abs(d.sum()) < 10 * np.abs(Xtz[:, i]).max() / rho   # the penalty leaves O(z / rho)
+
+
+def test_penalty_true_fit_matches_default_optimum(O, loop_case):
+    c, b, q0, p0 = loop_case
+    _, _, ll_pen, _, _ = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3, penalty=True)
+    _, _, ll_def, _, _ = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3)
+    assert ll_pen == pytest.approx(ll_def, rel=1e-6)
+    with pytest.raises(NotImplementedError):
+        O.fit(b, 3, q0, p0, n_iter=2, penalty=False)
