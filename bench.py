@@ -63,12 +63,14 @@ def parse(argv=None):
 
 
 def load_peaks():
+    """(hbm GB/s, bf16 TFLOP/s burst, bf16 TFLOP/s sustained, source)."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as f:
             d = json.load(f)
-        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
-    return 6800.0, 1900.0, "fallback"
+        return (d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0),
+                "measured")
+    return 6800.0, 1900.0, 1700.0, "fallback"
 
 
 class ClockSampler:
@@ -134,6 +136,20 @@ def pass_bytes(kind, I, J, K):
     if kind == "loglik":
         return geno + qp
     return None
+
+
+def pass_flops(I, J, K):
+    """Algorithmic FLOPs of one accumulation pass: the Hessian contraction
+    F_H = 2 N 4 K(K+1)/2 (symmetric part) and the gradient 2 N 4K, N = I J pairs."""
+    n = float(I) * J
+    return 2.0 * n * 4 * K * (K + 1) / 2, 2.0 * n * 4 * K
+
+
+# DRAM bytes (read + write) per (individual, block) pair of the tensor-core
+# Hessian passes, from one-pass ncu captures of one launch each at I=100,000,
+# J=100,000, K=8 (profiles/k_accum_tc_c3_dram.md): P 5.65 GB, Q 5.83 GB per
+# launch over 1e10 pairs.
+TRAFFIC_PER_PAIR = {"accum_q": 0.583, "accum_p": 0.565}
 
 
 def workload(name, cfg):
@@ -274,17 +290,42 @@ def run_ours(args, world, rank, local):
     iters = timed[-1]["iters"]
     ll = timed[-1]["ll"]
 
-    # roofline of the dominant pass kernel
-    peak_hbm, peak_bf16, peak_src = load_peaks()
+    # roofline of the dominant pass kernel.  The accumulation passes are
+    # contractions on the tensor cores: their roofline is the tensor pipe
+    # (achieved = Hessian FLOPs / time against the measured sustained bf16
+    # peak, the kernel running inside a long fit), with the HBM floor as the
+    # secondary bound.  The log-likelihood pass streams the class words (HBM).
+    peak_hbm, peak_bf16, peak_bf16_sus, peak_src = load_peaks()
     top = max(("accum_q", "accum_p", "loglik"), key=lambda k: stats[k][1])
     n_top, ms_top = stats[top]
-    per_launch_ms = ms_top / max(n_top, 1)
+    # passes of the top kind: in the mixed method a tensor-core pass is two
+    # launches (operand image, pass); the gradient-only EM Q passes run on the
+    # CUDA cores (one launch each)
+    passes = n_top
+    if args.precision == "mixed" and top == "accum_p":
+        passes = n_top / 2
+    elif args.precision == "mixed" and top == "accum_q":
+        em = args.em_iters * args.steps
+        passes = (n_top - em) / 2 + em
+    per_launch_ms = ms_top / max(passes, 1)
     alg = pass_bytes(top, I, J, K)
-    achieved = alg / (per_launch_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak_hbm, "unit": "GB/s",
-                "frac": achieved / peak_hbm, "traffic": None, "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
-                "share_of_timed": ms_top / (ms * args.steps)}
+    hbm_gbs = alg / (per_launch_ms * 1e-3) / 1e9
+    if top in ("accum_q", "accum_p"):
+        fh, fg = pass_flops(I, J, K)
+        achieved = fh / (per_launch_ms * 1e-3) / 1e12
+        traffic = TRAFFIC_PER_PAIR[top] * I * J if args.precision == "mixed" else None
+        roofline = {"bound": "tensor", "kernel": top, "achieved": achieved, "peak": peak_bf16_sus,
+                    "unit": "TFLOP/s", "frac": achieved / peak_bf16_sus, "traffic": traffic,
+                    "peak_source": peak_src + " (bf16 sustained)", "flops_hessian_per_launch": fh,
+                    "flops_gradient_per_launch": fg, "ms_per_launch": per_launch_ms,
+                    "secondary_hbm": {"achieved": hbm_gbs, "peak": peak_hbm, "unit": "GB/s",
+                                      "frac": hbm_gbs / peak_hbm, "algorithmic_bytes_per_launch": alg},
+                    "share_of_timed": ms_top / (ms * args.steps)}
+    else:
+        roofline = {"bound": "hbm", "kernel": top, "achieved": hbm_gbs, "peak": peak_hbm, "unit": "GB/s",
+                    "frac": hbm_gbs / peak_hbm, "traffic": None, "peak_source": peak_src,
+                    "algorithmic_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
+                    "share_of_timed": ms_top / (ms * args.steps)}
     kernels = {k: {"launches": n, "ms": round(t, 3)} for k, (n, t) in stats.items()}
 
     line = {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
