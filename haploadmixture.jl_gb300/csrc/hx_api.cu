@@ -897,6 +897,115 @@ int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int
     return first;
 }
 
+// ------------------------------------------------------------ learned warm start
+namespace {
+struct LwsScratch {   // temporary device buffers of one training or gradient call
+    float* part = nullptr;
+    double* loss_part = nullptr;
+    float* grad = nullptr;
+    int64_t* idx = nullptr;
+    ~LwsScratch() {
+        if (part) cudaFree(part);
+        if (loss_part) cudaFree(loss_part);
+        if (grad) cudaFree(grad);
+        if (idx) cudaFree(idx);
+    }
+    cudaError_t alloc(int64_t nidx) {
+        cudaError_t e = cudaMalloc((void**)&part, (size_t)LWS_MAX_BLOCKS * HX_LWS_NPARAM * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&loss_part, LWS_MAX_BLOCKS * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&grad, HX_LWS_NPARAM * sizeof(float));
+        if (e == cudaSuccess && nidx > 0) e = cudaMalloc((void**)&idx, (size_t)nidx * sizeof(int64_t));
+        return e;
+    }
+};
+int cuda_status(cudaError_t e) {
+    return e == cudaSuccess ? HX_OK : (e == cudaErrorMemoryAllocation ? HX_ENOMEM : HX_ECUDA);
+}
+}  // namespace
+
+int hx_lws_features(hx_ctx* c, float* d_feat) {
+    HX_ST(check_qp(c));
+    if (!d_feat) return HX_EINVAL;
+    HX_CK(cudaSetDevice(c->device));
+    HX_ST(pass_q(c, qof(c->x), pof(c, c->x), false, c->XtXq, c->Xtzq));
+    PassArgs a = pass_args(c, qof(c->x), pof(c, c->x));
+    HX_LAUNCH(HX_KIND_OTHER, 1, lws_features(c->K, a, c->dm, c->Xtzq, d_feat, c->st));
+    HX_CK(cudaStreamSynchronize(c->st));
+    return HX_OK;
+}
+
+int hx_lws_forward(const float* d_feat, int64_t n, int32_t K, const float* d_params, float* d_q, void* stream) {
+    if (!d_feat || !d_params || !d_q || n < 0 || K < 1 || K > HX_KMAX) return HX_EINVAL;
+    if (n == 0) return HX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = lws_forward(d_feat, n, K, d_params, d_q, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e);
+}
+
+int hx_lws_grad(const float* d_feat, const float* d_target, int64_t n, int32_t K, const float* d_params,
+                float* d_grad, double* d_loss, void* stream) {
+    if (!d_feat || !d_target || !d_params || !d_grad || n <= 0 || K < 1 || K > HX_KMAX) return HX_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = lws_attrs();
+    LwsScratch sc;
+    if (e == cudaSuccess) e = sc.alloc(0);
+    if (e == cudaSuccess) e = lws_grad(d_feat, d_target, nullptr, n, K, d_params, sc.part, sc.loss_part, d_grad, d_loss, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e);
+}
+
+int hx_lws_train(const float* d_feat, const float* d_target, int64_t n, int32_t K, float* d_params, float* d_m,
+                 float* d_v, int32_t steps, int64_t batch, float lr, uint64_t seed, int32_t step0, double* d_losses,
+                 void* stream) {
+    if (!d_feat || !d_target || !d_params || !d_m || !d_v || n <= 0 || K < 1 || K > HX_KMAX || steps < 0 ||
+        batch <= 0 || step0 < 0)
+        return HX_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = lws_attrs();
+    LwsScratch sc;
+    if (e == cudaSuccess) e = sc.alloc(batch);
+    if (e == cudaSuccess)
+        e = lws_train(d_feat, d_target, n, K, d_params, d_m, d_v, steps, batch, lr, seed, step0, sc.idx, sc.part,
+                      sc.loss_part, sc.grad, d_losses, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e);
+}
+
+int hx_lws_warm_start(hx_ctx* c, const float* params, int32_t* accepted) {
+    HX_ST(check_qp(c));
+    if (!params) return HX_EINVAL;
+    if (accepted) *accepted = 0;
+    HX_CK(cudaSetDevice(c->device));
+    const int64_t nq = (int64_t)c->K * c->I;
+    Tmp t;
+    int st = HX_OK;
+    float* dP = t.get<float>(c, HX_LWS_NPARAM, &st);
+    float* feat = t.get<float>(c, (size_t)nq * 2, &st);
+    float* qf = t.get<float>(c, (size_t)nq, &st);
+    if (st != HX_OK) return st;
+    HX_CK(cudaMemcpyAsync(dP, params, HX_LWS_NPARAM * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    HX_ST(hx_lws_features(c, feat));
+    HX_CK(lws_forward(feat, c->I, c->K, dP, qf, c->st));
+    // x_tmp = [project(q') | p]
+    HX_LAUNCH(HX_KIND_OTHER, 1, launch_f2d(qf, nq, qof(c->xt), c->st));
+    HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_q(qof(c->xt), nullptr, c->K, c->I, c->eps, qof(c->xt), c->st));
+    HX_CK(cudaMemcpyAsync(pof(c, c->xt), pof(c, c->x), (size_t)c->K * 4 * c->J * sizeof(double),
+                          cudaMemcpyDeviceToDevice, c->st));
+    HX_ST(loglik_to_slot(c, qof(c->x), pof(c, c->x), S_TMP));
+    HX_ST(read_slots(c));
+    const double ll0 = c->h_slots[S_TMP];
+    HX_ST(loglik_to_slot(c, qof(c->xt), pof(c, c->xt), S_TMP));
+    HX_ST(read_slots(c));
+    const double ll1 = c->h_slots[S_TMP];
+    if (ll1 > ll0) {
+        HX_CK(cudaMemcpyAsync(c->x, c->xt, (size_t)c->nx * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        HX_ST(reset_state(c));
+        if (accepted) *accepted = 1;
+    }
+    return HX_OK;
+}
+
 int hx_fit(hx_ctx* c, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_info* info) {
     HX_ST(check_qp(c));
     auto t0 = std::chrono::steady_clock::now();

@@ -715,6 +715,14 @@ cudaError_t launch_step_p(const double* p, const double* d, int K, int64_t J, do
     k_step_p<<<nblk((int64_t)K * J, 128), 128, 0, st>>>(p, d, K, J, eps, out, factor);
     return cudaGetLastError();
 }
+__global__ void k_f2d(const float* __restrict__ a, int64_t n, double* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = (double)a[t];
+}
+cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st) {
+    k_f2d<<<nblk(n, 256), 256, 0, st>>>(a, n, out);
+    return cudaGetLastError();
+}
 cudaError_t init_kernel_attrs() {
     return cudaFuncSetAttribute(k_qp_p, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(QP_WARPS * qp_warp_bytes(4 * HX_KMAX)));

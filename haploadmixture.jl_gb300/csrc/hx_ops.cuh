@@ -40,6 +40,20 @@ cudaError_t tc_run_g3(TcCall& c);   // K = 10
 cudaError_t tc_run_g4(TcCall& c);   // K = 11
 cudaError_t tc_run_g5(TcCall& c);   // K = 12
 cudaError_t init_tc_attrs();
+
+cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st);
+
+// learned warm start (hx_lws.cu)
+cudaError_t lws_attrs();
+cudaError_t lws_features(int K, const PassArgs& a, const unsigned long long* dm, const double* Xtz, float* feat,
+                         cudaStream_t st);
+cudaError_t lws_forward(const float* feat, int64_t n, int K, const float* P, float* q, cudaStream_t st);
+cudaError_t lws_grad(const float* feat, const float* target, const int64_t* idx, int64_t ns, int K, const float* P,
+                     float* part, double* loss_part, float* grad, double* loss, cudaStream_t st);
+cudaError_t lws_train(const float* feat, const float* target, int64_t n, int K, float* P, float* m, float* v,
+                      int steps, int64_t bs, float lr, uint64_t seed, int step0, int64_t* idx, float* part,
+                      double* loss_part, float* grad, double* losses, cudaStream_t st);
+constexpr int LWS_MAX_BLOCKS = 304;   // CTA partials of lws_grad
 cudaError_t launch_accum_q_tc(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_p_tc(int K, bool hess, const PassArgs& a, cudaStream_t st);
 size_t tc_image_bytes(int K, int64_t I, int64_t J);

@@ -182,6 +182,38 @@ int hx_fit(hx_ctx* ctx, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_in
  * hx_fit alone.  status (optional, n entries) receives each fit's status;
  * the return value is the first non-OK status, or HX_OK. */
 int hx_create_shared(const hx_ctx* parent, int32_t K, const hx_opts* opts, hx_ctx** out);
+/* Learned warm start of Q (no reference counterpart; BASELINE configuration 5).
+ * Features of (individual i, ancestry k), two FP32 values each, feat[i][k][2]:
+ *   f1 = a_k - max_k' a_k', a_k = (1/n_i) sum_j log L_ij(Q_i = e_k)
+ *   f2 = (g - 1) sqrt(n_i), g = Xtz_q[k,i] / (2 n_i) (Q gradient per block),
+ *   n_i = J - dm_i.
+ * Network, permutation-equivariant over k, FP16 weights and FP32 accumulation:
+ *   h1_k = relu(W1 x_k + b1), m = mean_k h1_k, h2_k = relu(W2 h1_k + U2 m + b2),
+ *   z_k = w3.h2_k + b3, q = softmax(z).  Parameters: FP32 master copy, layout
+ *   W1[64][2], b1[64], W2[64][64], U2[64][64], b2[64], w3[64], b3 (HX_LWS_NPARAM
+ *   floats, zero-padded).  Loss: cross-entropy against converged Q.
+ * Device pointers unless stated; stream may be NULL. */
+#define HX_LWS_HIDDEN 64
+#define HX_LWS_NPARAM 8516
+/* Features at the context's current state (device, I*K*2 floats). */
+int hx_lws_features(hx_ctx* ctx, float* d_feat);
+/* q[i][k] for n samples of K ancestries. */
+int hx_lws_forward(const float* d_feat, int64_t n, int32_t K, const float* d_params, float* d_q, void* stream);
+/* Mean loss and its gradient over all n samples (d_grad: HX_LWS_NPARAM floats). */
+int hx_lws_grad(const float* d_feat, const float* d_target, int64_t n, int32_t K, const float* d_params,
+                float* d_grad, double* d_loss, void* stream);
+/* `steps` Adam steps (lr, beta 0.9/0.999) on mini-batches of `batch` samples
+ * drawn with replacement by a counter-based hash of (seed, step0 + s, slot);
+ * d_m, d_v: Adam moments (HX_LWS_NPARAM floats each, zero at the start);
+ * d_losses (optional): mean loss of each step's batch, before the update. */
+int hx_lws_train(const float* d_feat, const float* d_target, int64_t n, int32_t K, float* d_params, float* d_m,
+                 float* d_v, int32_t steps, int64_t batch, float lr, uint64_t seed, int32_t step0, double* d_losses,
+                 void* stream);
+/* Warm start: Q' = project(network(features of the current state)) replaces Q
+ * if it raises the log-likelihood at the current P; then the QN history is
+ * reset (hx_set_qp semantics).  params: host, HX_LWS_NPARAM floats.
+ * *accepted (optional) = 1 if Q was replaced. */
+int hx_lws_warm_start(hx_ctx* ctx, const float* params, int32_t* accepted);
 int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int32_t em_iters, int32_t threads,
                 hx_fit_info* infos, int32_t* status);
 
