@@ -209,7 +209,8 @@ int loglik_to_slot(hx_ctx* c, const double* q, const double* p, int slot) {
     } else {
         HX_LAUNCH(HX_KIND_LOGLIK, 1, launch_loglik_f32x2(c->K, a, c->st));
         HX_LAUNCH(HX_KIND_OTHER, 1,
-                  launch_reduce_sum(c->part_ll, (int64_t)loglik_f32x2_blocks(c->Ipad) * c->S_q, c->slots + slot, c->st));
+                  launch_reduce_sum(c->part_ll, (int64_t)loglik_f32x2_blocks(c->Ipad, c->K) * c->S_q, c->slots + slot,
+                                    c->st));
     }
     return HX_OK;
 }

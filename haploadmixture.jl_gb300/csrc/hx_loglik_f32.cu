@@ -5,11 +5,17 @@
 
 namespace hx {
 
-int loglik_f32x2_blocks(int64_t Ipad) { return (int)((Ipad + 2 * ACC_THREADS - 1) / (2 * ACC_THREADS)); }
+// individuals per thread (4 measured slower at K = 8: 155 registers cut the
+// resident warps from 20 to 12 per SM)
+inline int loglik_nu(int) { return 2; }
+int loglik_f32x2_blocks(int64_t Ipad, int K) {
+    const int64_t per = (int64_t)loglik_nu(K) * ACC_THREADS;
+    return (int)((Ipad + per - 1) / per);
+}
 
 cudaError_t launch_loglik_f32x2(int K, const PassArgs& a, cudaStream_t st) {
-    dim3 grid((unsigned)loglik_f32x2_blocks(a.Ipad), (unsigned)a.S);
-#define HX_CASE(KK) case KK: k_loglik2<KK><<<grid, ACC_THREADS, 0, st>>>(a); break;
+    dim3 grid((unsigned)loglik_f32x2_blocks(a.Ipad, K), (unsigned)a.S);
+#define HX_CASE(KK) case KK: k_loglik2<KK, 2><<<grid, ACC_THREADS, 0, st>>>(a); break;
     switch (K) { HX_FOR_K(HX_CASE) default: return cudaErrorInvalidValue; }
 #undef HX_CASE
     return cudaGetLastError();

@@ -18,8 +18,8 @@ cudaError_t launch_loglik_f64(int K, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_q_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_accum_p_f32(int K, bool hess, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
-cudaError_t launch_loglik_f32x2(int K, const PassArgs& a, cudaStream_t st);   // two individuals per thread
-int loglik_f32x2_blocks(int64_t Ipad);
+cudaError_t launch_loglik_f32x2(int K, const PassArgs& a, cudaStream_t st);   // several individuals per thread
+int loglik_f32x2_blocks(int64_t Ipad, int K);
 
 // tensor-core (tcgen05) Hessian+gradient passes of the mixed method (hx_tc.cu)
 // Host operations on the tensor-core instantiation of one K (hx_tc_impl.cuh);

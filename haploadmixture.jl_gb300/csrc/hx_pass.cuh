@@ -320,13 +320,13 @@ k_loglik(PassArgs a) {
 
 // ------------------------------------------------------------------ loglik, FP32
 // The mixed method's log-likelihood pass (same sums as k_loglik<K, float>):
-// each thread carries two individuals (i and i + ACC_THREADS) that share every
+// each thread carries NU individuals (i + u ACC_THREADS) that share every
 // staged p row, and forms qp for haplotype pairs (h, h+1) with packed FP32x2
 // FMAs (fma.rn.f32x2: two IEEE FMAs per instruction, the same results and
 // order as fmaf).  Stage rows are transposed to [block][k][h] so that one
 // 16-byte load gives p[k, 4j..4j+3].
 
-template <int K>
+template <int K, int NU>
 __global__ void __launch_bounds__(ACC_THREADS)
 k_loglik2(PassArgs a) {
     __shared__ __align__(16) float spt[QSTAGE_WORDS * 8 * 4 * K];
@@ -334,25 +334,27 @@ k_loglik2(PassArgs a) {
     __shared__ float4 s_snp[4];
     const int tid = threadIdx.x;
     snp_table_init(s_snp, tid);
-    int64_t ii[2];
-    ii[0] = (int64_t)blockIdx.x * 2 * ACC_THREADS + tid;
-    ii[1] = ii[0] + ACC_THREADS;
+    int64_t ii[NU];
+#pragma unroll
+    for (int u = 0; u < NU; ++u) ii[u] = (int64_t)blockIdx.x * NU * ACC_THREADS + u * ACC_THREADS + tid;
     const int w0 = blockIdx.y * a.per_chunk;
     const int w1 = min(a.JW, w0 + a.per_chunk);
-    uint64_t qd[2][K];
-    float mant[2] = {1.f, 1.f};
-    int ex[2] = {0, 0};
-    bool zero[2] = {false, false}, bad[2] = {false, false};
+    uint64_t qd[NU][K];
+    float mant[NU];
+    int ex[NU];
+    bool zero[NU], bad[NU];
 #pragma unroll
-    for (int u = 0; u < 2; ++u)
+    for (int u = 0; u < NU; ++u) { mant[u] = 1.f; ex[u] = 0; zero[u] = false; bad[u] = false; }
+#pragma unroll
+    for (int u = 0; u < NU; ++u)
 #pragma unroll
         for (int k = 0; k < K; ++k)
             qd[u][k] = f2_dup(ii[u] < a.I ? (float)a.q[(int64_t)K * ii[u] + k] : 1.f / K);
     for (int ws = w0; ws < w1; ws += QSTAGE_WORDS) {
         const int nw = min(QSTAGE_WORDS, w1 - ws);
-        uint32_t words[2][QSTAGE_WORDS];
+        uint32_t words[NU][QSTAGE_WORDS];
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < NU; ++u)
 #pragma unroll
             for (int w = 0; w < QSTAGE_WORDS; ++w)
                 words[u][w] = (w < nw && ii[u] < a.Ipad) ? a.G[(int64_t)(ws + w) * a.Ipad + ii[u]] : HX_PAD_WORD;
@@ -369,18 +371,20 @@ k_loglik2(PassArgs a) {
 #pragma unroll 2
             for (int b = 0; b < 8; ++b) {
                 const ulonglong2* pb = reinterpret_cast<const ulonglong2*>(spt + (w * 8 + b) * 4 * K);
-                uint64_t z01[2] = {0ull, 0ull}, z23[2] = {0ull, 0ull};
+                uint64_t z01[NU], z23[NU];
+#pragma unroll
+                for (int u = 0; u < NU; ++u) { z01[u] = 0ull; z23[u] = 0ull; }
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
                     const ulonglong2 pk = pb[k];
 #pragma unroll
-                    for (int u = 0; u < 2; ++u) {
+                    for (int u = 0; u < NU; ++u) {
                         z01[u] = f2_fma(qd[u][k], pk.x, z01[u]);
                         z23[u] = f2_fma(qd[u][k], pk.y, z23[u]);
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
+                for (int u = 0; u < NU; ++u) {
                     const unsigned nib = (words[u][w] >> (4 * b)) & 0xFu;
                     float qp[4];
                     f2_split(z01[u], qp[0], qp[1]);
@@ -397,7 +401,7 @@ k_loglik2(PassArgs a) {
     }
     double v = 0.0;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < NU; ++u) {
         if (ii[u] < a.I) {
             double x = log((double)mant[u]) + (double)ex[u] * 0.69314718055994530942;
             if (zero[u]) x = -INFINITY;
