@@ -30,11 +30,11 @@
 // on an mbarrier with a transaction count.
 //
 // Pipeline per stage, with no CTA-wide barrier in the loop: every thread waits
-// for the stage's ring slot, waits until the MMAs that last read its A buffer
-// (stage s-2) are done, generates its part of the A tiles and arrives on a
-// shared counter; the last arriver issues the stage's MMAs, commits them to an
-// mbarrier, and refills the ring slot of stage s-1 once that stage's MMAs are
-// done.  Warps therefore run up to two stages apart, and two CTAs (16 warps)
+// for the stage's ring slot and until the MMAs that last read its A buffer
+// (stage s-2) are done; thread 0 then refills the ring slot of stage s-2 with
+// stage s-2+RING; every warp generates its part of the A tiles and arrives on
+// a shared counter; the last arriving warp issues the stage's MMAs and commits
+// them to an mbarrier.  Warps therefore run up to two stages apart, and two CTAs (16 warps)
 // share an SM.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
 // slots[S_TC_TIMEOUT] and the CTA drains and exits.
 #pragma once
@@ -432,18 +432,6 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int 
     else compensate<K, 1>(acc, comp);
 }
 
-// Ring refill by the stage-s issuer: the slot of stage s-1 receives stage
-// s-1+RING once the MMAs of stage s-1 (issued one stage earlier) are done.
-// Waiting here keeps the copies RING-1 stages ahead of their use; a non-blocking
-// test that defers the refill measured slower.
-template <class LOAD>
-__device__ __forceinline__ void refill_ring(Sync* sy, double* slots, int s, int ns, LOAD&& load_stage) {
-    if (s >= 1 && s - 1 + RING < ns) {
-        if (!mbar_wait(&sy->mma_done[(s - 1) & 1], ((s - 1) >> 1) & 1, TC_BUDGET)) set_bad(sy, slots);
-        else load_stage(s - 1 + RING);
-    }
-}
-
 // ------------------------------------------------------------------ Q side
 // CTA: 128 individuals (TMEM lanes) x a chunk of class words; stage = 1 word
 // (8 blocks, 32 haplotype columns).  Thread (r, hf): row r, blocks 4hf..4hf+3.
@@ -564,6 +552,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         if (s >= 2 && !is_bad(sy))
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         if (is_bad(sy)) break;
+        // ring refill: the slot of stage s-2 is free (its MMAs are done -- just
+        // waited for -- and they were issued after every thread had read it)
+        if (tid == 0 && s >= 2 && s - 2 + RING < ns) load_stage(s - 2 + RING);
         const uint32_t word = SW[slot * 128 + r];
         // this stage's qp: 16 columns of this thread's row
         float qpv[16];
@@ -615,7 +606,6 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, (s % TC_FLUSH) == 0);
             // mma_done also covers the qp MMA, so that draining it covers every MMA in flight
             commit_stage(sy, s, ns, b);
-            refill_ring(sy, a.slots, s, ns, load_stage);
             // the qp tile slot of stage s is free (its MMA is done: every thread waited for it)
             if (s + QRING < ns) load_qtile(s + QRING);
         }
@@ -745,6 +735,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         if (s >= 2 && !is_bad(sy))
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         if (is_bad(sy)) break;
+        // ring refill (see the Q side)
+        if (tid == 0 && s >= 2 && s - 2 + RING < ns) load_stage(s - 2 + RING);
         const float* Qs = reinterpret_cast<const float*>(smem + (sR - sA) + slot * GB + 2 * D::B_TILE);
         const uint32_t* Ws = SW + slot * 4 * KD + (jl >> 3) * KD;
         // A = W^T tile: rows m = 4*jl + h, reduction over the stage's individuals
@@ -791,7 +783,6 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
             const int d = (s / TC_FLUSH) & 1;
             issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, sR + slot * GB, (s % TC_FLUSH) == 0);
             commit_stage(sy, s, ns, b);
-            refill_ring(sy, a.slots, s, ns, load_stage);
         }
         maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
