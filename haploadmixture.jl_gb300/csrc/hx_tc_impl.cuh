@@ -73,6 +73,10 @@ template <int K> struct TcDims {
     static constexpr int TCOLS = (2 * NT <= 32) ? 32 : (2 * NT <= 64) ? 64 : (2 * NT <= 128) ? 128 : 256;
     static constexpr int HALF = NT / 2;
     static constexpr int B_TILE = (NT / 8) * SBO_STD;    // NT rows x 32 x 2 B
+    // P side, stacked operands: one TMEM window holds hi.hi (+ lo.hi) and hi.lo
+    // of the Hessian side by side, then the same for the gradient
+    static constexpr int WS = 2 * NHP + 2 * NG;
+    static constexpr int TCOLS_S = (2 * WS <= 32) ? 32 : (2 * WS <= 64) ? 64 : (2 * WS <= 128) ? 128 : (2 * WS <= 256) ? 256 : 512;
     // CTAs per SM: 2 while the generators fit in 128 registers, else 1
     static constexpr int MINB = K <= 8 ? 2 : 1;
 };
@@ -159,13 +163,37 @@ __device__ __forceinline__ void drain(Sync* sy) {
 // TMEM window fold: this thread's lane, columns [HF*HALF, HF*HALF + HALF) of the
 // accumulator at column base dcol.  Hessian columns add plainly; gradient
 // columns (>= NHP) use Kahan compensation in comp[col - NHP].
-template <int K, int HF>
+// With STACK (P side) logical column c sums two physical columns: c and
+// NHP + c for the Hessian, 2NHP + g and 2NHP + NG + g for gradient column g.
+template <int K, int HF, bool STACK>
 __device__ __forceinline__ void fold(uint32_t taddr_lane, int dcol, float* acc, float* comp) {
     using D = TcDims<K>;
     uint32_t raw[D::HALF];
+    if (!STACK) {
 #pragma unroll
-    for (int c = 0; c < D::HALF / 8; ++c) tmem_ld8_async(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), raw + 8 * c);
-    tmem_wait_ld();
+        for (int c = 0; c < D::HALF / 8; ++c)
+            tmem_ld8_async(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), raw + 8 * c);
+        tmem_wait_ld();
+    } else {
+#pragma unroll
+        for (int c = 0; c < D::HALF / 8; ++c) {
+            const int col = HF * D::HALF + 8 * c;     // chunks never straddle NHP (a multiple of 16)
+            const int p0 = col < D::NHP ? col : 2 * D::NHP + (col - D::NHP);
+            tmem_ld8_async(taddr_lane + (uint32_t)(dcol + p0), raw + 8 * c);
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < D::HALF / 8; ++c) {
+            const int col = HF * D::HALF + 8 * c;
+            const int p1 = col < D::NHP ? D::NHP + col : 2 * D::NHP + D::NG + (col - D::NHP);
+            uint32_t r2[8];
+            tmem_ld8_async(taddr_lane + (uint32_t)(dcol + p1), r2);
+            tmem_wait_ld();
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                raw[8 * c + t] = __float_as_uint(__uint_as_float(raw[8 * c + t]) + __uint_as_float(r2[t]));
+        }
+    }
 #pragma unroll
     for (int c = 0; c < D::HALF / 8; ++c) {
         float v[8];
@@ -185,10 +213,10 @@ __device__ __forceinline__ void fold(uint32_t taddr_lane, int dcol, float* acc, 
         }
     }
 }
-template <int K>
+template <int K, bool STACK>
 __device__ __forceinline__ void fold_half(int hf, uint32_t taddr_lane, int dcol, float* acc, float* comp) {
-    if (hf == 0) fold<K, 0>(taddr_lane, dcol, acc, comp);
-    else fold<K, 1>(taddr_lane, dcol, acc, comp);
+    if (hf == 0) fold<K, 0, STACK>(taddr_lane, dcol, acc, comp);
+    else fold<K, 1, STACK>(taddr_lane, dcol, acc, comp);
 }
 // Applies the Kahan compensation to the gradient columns: acc then holds the sums.
 template <int K, int HF>
@@ -214,20 +242,54 @@ __device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aB
     const uint32_t dG = tmem + dcol + D::NHP;
     const uint32_t bPPh = bBase, bPPl = bBase + D::B_TILE;
     const uint32_t bPh = bBase + (D::NHP / 8) * SBO_STD, bPl = bPh + D::B_TILE;
+    // descriptors of other addresses: the 14-bit address field (bytes >> 4)
+    // of one base descriptor plus the offset >> 4 (shared memory < 256 KB)
+    const uint64_t dA = sdesc(aBase, aLBO, aSBO), dB = sdesc(bBase, LBO_STD, SBO_STD);
+    const uint64_t oS = (uint64_t)(aStride >> 4), oBl = (uint64_t)(D::B_TILE >> 4);
+    const uint64_t oPh = (uint64_t)((bPh - bBase) >> 4);
+    (void)bPPh; (void)bPPl; (void)bPl;
 #pragma unroll
     for (int ks = 0; ks < KD / 16; ++ks) {
-        const uint32_t ao = ks * 2 * aLBO, bo = ks * 2 * LBO_STD;
+        const uint64_t ao = (uint64_t)((ks * 2 * aLBO) >> 4), bo = (uint64_t)((ks * 2 * LBO_STD) >> 4);
         const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
-        const uint64_t aWh = sdesc(aBase + ao, aLBO, aSBO), aWl = sdesc(aBase + aStride + ao, aLBO, aSBO);
-        const uint64_t aUh = sdesc(aBase + 2 * aStride + ao, aLBO, aSBO), aUl = sdesc(aBase + 3 * aStride + ao, aLBO, aSBO);
+        const uint64_t aWh = dA + ao, aWl = aWh + oS, aUh = aWh + 2 * oS, aUl = aWh + 3 * oS;
         if (HESS) {
-            mma_bf16(dH, aWh, sdesc(bPPh + bo, LBO_STD, SBO_STD), idH, acc0);
-            mma_bf16(dH, aWh, sdesc(bPPl + bo, LBO_STD, SBO_STD), idH, 1u);
-            mma_bf16(dH, aWl, sdesc(bPPh + bo, LBO_STD, SBO_STD), idH, 1u);
+            mma_bf16(dH, aWh, dB + bo, idH, acc0);
+            mma_bf16(dH, aWh, dB + oBl + bo, idH, 1u);
+            mma_bf16(dH, aWl, dB + bo, idH, 1u);
         }
-        mma_bf16(dG, aUh, sdesc(bPh + bo, LBO_STD, SBO_STD), idG, acc0);
-        mma_bf16(dG, aUh, sdesc(bPl + bo, LBO_STD, SBO_STD), idG, 1u);
-        mma_bf16(dG, aUl, sdesc(bPh + bo, LBO_STD, SBO_STD), idG, 1u);
+        mma_bf16(dG, aUh, dB + oPh + bo, idG, acc0);
+        mma_bf16(dG, aUh, dB + oPh + oBl + bo, idG, 1u);
+        mma_bf16(dG, aUl, dB + oPh + bo, idG, 1u);
+    }
+}
+
+// P side with stacked B rows [hi_H | lo_H | hi_G | lo_G] (one tile of 2 NT rows):
+// the hi.hi and hi.lo products come from one MMA each for the Hessian (N = 2NHP)
+// and the gradient (N = 2NG), into side-by-side TMEM columns; lo.hi adds into
+// the hi.hi columns.  Eight MMAs per 32-deep stage instead of twelve.
+template <int K, bool HESS>
+__device__ __forceinline__ void issue_stage_stacked(uint32_t tmem, int dcol, uint32_t aBase, int aStride, int aLBO,
+                                                    int aSBO, uint32_t bBase, bool first) {
+    using D = TcDims<K>;
+    constexpr uint32_t idH2 = idesc_bf16(2 * D::NHP), idH = idesc_bf16(D::NHP);
+    constexpr uint32_t idG2 = idesc_f16(2 * D::NG), idG = idesc_f16(D::NG);
+    const uint32_t dH = tmem + dcol;
+    const uint32_t dG = tmem + dcol + 2 * D::NHP;
+    const uint64_t dA = sdesc(aBase, aLBO, aSBO), dB = sdesc(bBase, LBO_STD, SBO_STD);
+    const uint64_t oS = (uint64_t)(aStride >> 4);
+    const uint64_t oG = (uint64_t)(((2 * D::NHP / 8) * SBO_STD) >> 4);
+#pragma unroll
+    for (int ks = 0; ks < KD / 16; ++ks) {
+        const uint64_t ao = (uint64_t)((ks * 2 * aLBO) >> 4), bo = (uint64_t)((ks * 2 * LBO_STD) >> 4);
+        const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
+        const uint64_t aWh = dA + ao, aWl = aWh + oS, aUh = aWh + 2 * oS, aUl = aWh + 3 * oS;
+        if (HESS) {
+            mma_bf16(dH, aWh, dB + bo, idH2, acc0);
+            mma_bf16(dH, aWl, dB + bo, idH, 1u);
+        }
+        mma_bf16(dG, aUh, dB + oG + bo, idG2, acc0);
+        mma_bf16(dG, aUl, dB + oG + bo, idG, 1u);
     }
 }
 
@@ -252,14 +314,23 @@ __device__ __forceinline__ void issue_qp(uint32_t tmem_col, uint32_t sAq, uint32
 // v[k] v[k2] (bf16 hi/lo), rows NHP.. NHP+K-1 the scaled vector (fp16 hi/lo),
 // other rows zero.  Row n's 16-byte hi chunk goes to
 // base + (n/8)*SBO + kg*LBO + (n%8)*16, the lo chunk B_TILE further.
-template <int K>
+// STACK (P side): physical rows [hi_H (NHP) | lo_H (NHP) | hi_G (NG) | lo_G (NG)]
+// in one tile of 2 NT rows instead of a hi tile and a lo tile.
+template <int K, bool STACK>
 __device__ __forceinline__ void put_b_row(uint8_t* base, int kg, int n, const uint32_t (&h)[4], const uint32_t (&l)[4]) {
-    uint8_t* d = base + (n >> 3) * SBO_STD + kg * LBO_STD + (n & 7) * 16;
-    *reinterpret_cast<uint4*>(d) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4*>(d + TcDims<K>::B_TILE) = make_uint4(l[0], l[1], l[2], l[3]);
+    using D = TcDims<K>;
+    int ph = n, pl = n;
+    if (STACK) {
+        ph = n < D::NHP ? n : 2 * D::NHP + (n - D::NHP);
+        pl = n < D::NHP ? D::NHP + n : 2 * D::NHP + D::NG + (n - D::NHP);
+    }
+    uint8_t* dh = base + (ph >> 3) * SBO_STD + kg * LBO_STD + (ph & 7) * 16;
+    uint8_t* dl = STACK ? base + (pl >> 3) * SBO_STD + kg * LBO_STD + (pl & 7) * 16 : dh + D::B_TILE;
+    *reinterpret_cast<uint4*>(dh) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(dl) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-template <int K>
+template <int K, bool STACK>
 __device__ __forceinline__ void write_b_rows(const float (&v)[8][K], uint8_t* base, int kg) {
     using D = TcDims<K>;
 #pragma unroll
@@ -270,11 +341,11 @@ __device__ __forceinline__ void write_b_rows(const float (&v)[8][K], uint8_t* ba
 #pragma unroll
             for (int e = 0; e < 4; ++e)
                 split2(v[2 * e][k] * v[2 * e][k2], v[2 * e + 1][k] * v[2 * e + 1][k2], h[e], l[e]);
-            put_b_row<K>(base, kg, tri_idx<K>(k, k2), h, l);
+            put_b_row<K, STACK>(base, kg, tri_idx<K>(k, k2), h, l);
         }
     }
     const uint32_t z[4] = {0u, 0u, 0u, 0u};
-    for (int n = D::NH; n < D::NHP; ++n) put_b_row<K>(base, kg, n, z, z);
+    for (int n = D::NH; n < D::NHP; ++n) put_b_row<K, STACK>(base, kg, n, z, z);
 #pragma unroll
     for (int kk = 0; kk < D::NG; ++kk) {
         uint32_t h[4], l[4];
@@ -285,7 +356,7 @@ __device__ __forceinline__ void write_b_rows(const float (&v)[8][K], uint8_t* ba
             const float a1 = kk < K ? v[2 * e + 1][kc] * GB_SCALE : 0.f;
             split2_f16(a0, a1, h[e], l[e]);
         }
-        put_b_row<K>(base, kg, D::NHP + kk, h, l);
+        put_b_row<K, STACK>(base, kg, D::NHP + kk, h, l);
     }
 }
 
@@ -309,7 +380,7 @@ __global__ void __launch_bounds__(128) k_qimg(const double* __restrict__ p, int6
             const int64_t g = (32 * jw + 8 * kg + e) * K + k;
             v[e][k] = g < plimit ? (float)p[g] : 0.25f;
         }
-    write_b_rows<K>(v, base, kg);
+    write_b_rows<K, false>(v, base, kg);
     // tf32 hi/lo p tile of the qp MMA: rows m (32), reduction k (KP, zero-padded)
     uint8_t* bq = base + 2 * TcDims<K>::B_TILE;
 #pragma unroll
@@ -345,7 +416,7 @@ __global__ void __launch_bounds__(128) k_pimg(const double* __restrict__ q, int6
 #pragma unroll
         for (int k = 0; k < K; ++k) v[e][k] = i < I ? (float)q[(int64_t)K * i + k] : 1.f / K;
     }
-    write_b_rows<K>(v, base, kg);
+    write_b_rows<K, true>(v, base, kg);
     float* rows = reinterpret_cast<float*>(base + 2 * TcDims<K>::B_TILE);
 #pragma unroll
     for (int e = 0; e < 8; ++e)
@@ -393,26 +464,28 @@ __device__ __forceinline__ void commit_stage(Sync* sy, int s, int ns, int b) {
 // and before window w+2 reuses its columns (issued at stage (w+2)*TC_FLUSH,
 // once every thread has arrived there).
 constexpr int FOLD_OFF = TC_FLUSH / 2;
-template <int K>
+template <int K, bool STACK>
 __device__ __forceinline__ void maybe_fold(Sync* sy, double* slots, int hf, int s, uint32_t taddr_lane, float* acc,
                                            float* comp) {
     using D = TcDims<K>;
+    constexpr int WC = STACK ? D::WS : D::NT;   // TMEM columns per window
     if (s >= TC_FLUSH + FOLD_OFF && (s - FOLD_OFF) % TC_FLUSH == 0) {
         const int wp = (s - FOLD_OFF) / TC_FLUSH - 1;
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
         if (!ok) set_bad(sy, slots);
         else {
             fence_after();
-            fold_half<K>(hf, taddr_lane, (wp & 1) * D::NT, acc, comp);
+            fold_half<K, STACK>(hf, taddr_lane, (wp & 1) * WC, acc, comp);
         }
         fence_before();
     }
 }
 
-template <int K>
+template <int K, bool STACK>
 __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int ns, uint32_t taddr_lane, float* acc,
                                            float* comp) {
     using D = TcDims<K>;
+    constexpr int WC = STACK ? D::WS : D::NT;
     __syncthreads();
     if (ns > 0 && !is_bad(sy)) {
         // windows not folded in the loop: the last one and possibly the one before
@@ -422,7 +495,7 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int 
             const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[w & 1], (w >> 1) & 1, TC_BUDGET));
             if (!ok) { set_bad(sy, slots); break; }
             fence_after();
-            fold_half<K>(hf, taddr_lane, (w & 1) * D::NT, acc, comp);
+            fold_half<K, STACK>(hf, taddr_lane, (w & 1) * WC, acc, comp);
         }
     }
     drain(sy);
@@ -609,9 +682,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             // the qp tile slot of stage s is free (its MMA is done: every thread waited for it)
             if (s + QRING < ns) load_qtile(s + QRING);
         }
-        maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
+        maybe_fold<K, false>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
-    final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
+    final_fold<K, false>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
     // write partials: v < K gradient, v = K + tri index Hessian
     constexpr int NV = K + (HESS ? D::NH : 0);
     double* out = a.part + (int64_t)blockIdx.y * NV * a.Ipad;
@@ -698,7 +771,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         sy->loaded = t + 1;
     };
 
-    if (warp == 0) tmem_alloc<D::TCOLS>(&sy->tslot);
+    if (warp == 0) tmem_alloc<D::TCOLS_S>(&sy->tslot);
     init_sync(sy, tid);
     if (tid == 0) {
         sy->img0 = a.img + g0 * GB;
@@ -781,12 +854,13 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         if (arrive_last(&sy->arrived[b])) {
             fence_after();
             const int d = (s / TC_FLUSH) & 1;
-            issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, sR + slot * GB, (s % TC_FLUSH) == 0);
+            issue_stage_stacked<K, HESS>(tmem, d * D::WS, aB, A_TILE_PAD, LBO_PAD, SBO_PAD, sR + slot * GB,
+                                         (s % TC_FLUSH) == 0);
             commit_stage(sy, s, ns, b);
         }
-        maybe_fold<K>(sy, a.slots, hf, s, taddr_lane, acc, comp);
+        maybe_fold<K, true>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
-    final_fold<K>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
+    final_fold<K, true>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
     // rows m of this CTA: TMEM lane r
     const int r = tid & 127;
     const int64_t m = (int64_t)blockIdx.x * 128 + r;
@@ -816,7 +890,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
     }
     if (warp == 0) {
         fence_after();
-        tmem_dealloc<D::TCOLS>(tmem);
+        tmem_dealloc<D::TCOLS_S>(tmem);
     }
 }
 
