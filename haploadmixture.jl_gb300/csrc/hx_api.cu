@@ -295,7 +295,8 @@ int update_q(hx_ctx* c, bool update2) {
     return step_control(c, out, p, false, step);
 }
 
-// update_p! (src/algorithms_inner.jl:224-355), penalty branch (the default).
+// update_p! (src/algorithms_inner.jl:224-355): penalty branch by default, the
+// equality branch (K equalities per block, :307-310) with penalty = 0.
 int update_p(hx_ctx* c, bool update2) {
     double* q = update2 ? qof(c->xn2) : qof(c->xn);
     double* p = update2 ? pof(c, c->xn) : pof(c, c->x);
@@ -306,7 +307,8 @@ int update_p(hx_ctx* c, bool update2) {
     }
     HX_ST(pass_p(c, q, p, true, c->XtXp, c->Xtzp));
     HX_LAUNCH(HX_KIND_QP_P, 1,
-              launch_qp_p(c->K, c->J, c->XtXp, c->Xtzp, p, c->rho, pof(c, c->xt), c->slots, c->qp_ws, c->st));
+              launch_qp_p(c->K, c->J, c->XtXp, c->Xtzp, p, c->rho, pof(c, c->xt), c->slots, c->qp_ws, c->st,
+                          c->lo.penalty == 0));
     auto step = [&](double f) {
         HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_p(p, pof(c, c->xt), c->K, c->J, c->eps, out, c->st, f));
         return HX_OK;
@@ -481,9 +483,7 @@ int hx_loop_opts_default(hx_loop_opts* o) {
 
 int hx_set_loop_opts(hx_ctx* c, const hx_loop_opts* o) {
     if (!c || !o) return HX_EINVAL;
-    if (o->penalty == 0)
-        return fail(c, HX_EUNSUPPORTED, "penalty = 0 (P-step equality form, algorithms_inner.jl:306-310) is not built");
-    if (o->penalty != -1 && o->penalty != 1) return fail(c, HX_EINVAL, "penalty must be -1, 0 or 1");
+    if (o->penalty < -1 || o->penalty > 1) return fail(c, HX_EINVAL, "penalty must be -1, 0 or 1");
     c->lo = *o;
     return HX_OK;
 }
@@ -684,7 +684,7 @@ int hx_qp_q(hx_ctx* c, int64_t n, const double* XtX, const double* Xtz, const do
     HX_CK(cudaMemcpyAsync(dX, XtX, (size_t)K * K * n * 8, cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaMemcpyAsync(dz, Xtz, (size_t)K * n * 8, cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaMemcpyAsync(dq, q, (size_t)K * n * 8, cudaMemcpyHostToDevice, c->st));
-    HX_CK(launch_qp_q(K, n, dX, dz, dq, dd, c->slots, c->st));
+    HX_CK(launch_qp_q(K, n, dX, dz, dq, dd, c->slots, c->st, c->lo.penalty == 1 ? c->rho : -1.0));
     HX_CK(cudaMemcpyAsync(qdiff, dd, (size_t)K * n * 8, cudaMemcpyDeviceToHost, c->st));
     HX_CK(cudaStreamSynchronize(c->st));
     return HX_OK;
@@ -703,7 +703,7 @@ int hx_qp_p(hx_ctx* c, int64_t n, const double* XtX, const double* Xtz, const do
     HX_CK(cudaMemcpyAsync(dX, XtX, (size_t)K * K * 4 * n * 8, cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaMemcpyAsync(dz, Xtz, (size_t)K * 4 * n * 8, cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaMemcpyAsync(dp, p, (size_t)K * 4 * n * 8, cudaMemcpyHostToDevice, c->st));
-    HX_CK(launch_qp_p(K, n, dX, dz, dp, c->rho, dd, c->slots, nullptr, c->st));
+    HX_CK(launch_qp_p(K, n, dX, dz, dp, c->rho, dd, c->slots, nullptr, c->st, c->lo.penalty == 0));
     HX_CK(cudaMemcpyAsync(pdiff, dd, (size_t)K * 4 * n * 8, cudaMemcpyDeviceToHost, c->st));
     HX_CK(cudaStreamSynchronize(c->st));
     return HX_OK;

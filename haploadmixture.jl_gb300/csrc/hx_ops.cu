@@ -241,11 +241,16 @@ __global__ void k_step_p(const double* __restrict__ p, const double* __restrict_
 
 // ------------------------------------------------------------------ QP
 // One warp per problem: exact minimiser of 0.5 d'Hd - z'd subject to
-// lo <= d <= hi (and sum d = 0 when eq), by the primal active-set method of
-// the oracle (same working-set rules, tie-breaks and tolerance).  The free
+// lo <= d <= hi and G equality groups (G = 0: none; G = 1: sum d = 0;
+// G >= 2: the variables a with a % G == k sum to 0, for every k), by the
+// primal active-set method of the oracle (same working-set rules, tie-breaks
+// and tolerance).  The free
 // block of H is factorised by a warp-parallel right-looking Cholesky in
 // shared memory.  Restates OpenADMIXTURE's create_tableau!/quadratic_program!
-// contract as called at src/algorithms_inner.jl:160-166 and :303-305.
+// contract as called at src/algorithms_inner.jl:160-166, :303-305 and
+// :307-310 (the P quartets' K equalities).  With G >= 2 the multipliers come
+// from the G x G Schur system S nu = E_F y1 + E_X d_X, S = E_F H_FF^-1 E_F',
+// and a group's last free variable (fixed by its equality) never blocks.
 // GB300's FP64 unit is narrow and every lane's FP64 operation costs issue
 // slots on it, so each scalar step (square root, pivot reciprocal, the
 // solved unknown of a triangular sweep) is computed by lane 0 alone and
@@ -257,6 +262,7 @@ enum { QF = 0, QL = 1, QH = 2 };
 struct QPWork {
     double* A;
     double *d, *z, *lo, *hi, *r, *y1, *y2, *ds, *g, *iv;
+    double *Y, *S, *nu, *rhs;   // G >= 2 only: nF x G, G x G, G, G
     int *st, *F;
 };
 
@@ -294,14 +300,42 @@ __device__ void tri_solve(const double* A, const double* iv, int nF, double* x, 
     __syncwarp();
 }
 
-template <class HF>
-__device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
+// L L' X = B in place for the ncol columns of X (nF x ncol, column-major).
+__device__ void tri_solve_cols(const double* A, const double* iv, int nF, double* X, int ncol, int lane) {
+    for (int a = 0; a < nF; ++a) {
+        __syncwarp();
+        for (int c = lane; c < ncol; c += 32) X[a + nF * c] *= iv[a];
+        __syncwarp();
+        const int m = nF - a - 1;
+        for (int e = lane; e < m * ncol; e += 32) {
+            const int rr = a + 1 + e % m, c = e / m;
+            X[rr + nF * c] -= A[rr + nF * a] * X[a + nF * c];
+        }
+    }
+    for (int a = nF - 1; a >= 0; --a) {
+        __syncwarp();
+        for (int c = lane; c < ncol; c += 32) X[a + nF * c] *= iv[a];
+        __syncwarp();
+        for (int e = lane; e < a * ncol; e += 32) {
+            const int rr = e % a, c = e / a;
+            X[rr + nF * c] -= A[a + nF * rr] * X[a + nF * c];
+        }
+    }
+    __syncwarp();
+}
+
+// GROUPS: the G-group path (G >= 2, instantiated apart so that the other
+// forms keep their register allocation); otherwise G is 0 or 1.
+template <bool GROUPS, class HF>
+__device__ int warp_qp(int n, int G, const HF& H, const QPWork& w) {
     const int lane = threadIdx.x & 31;
     double zs = 1.0;
     for (int a = lane; a < n; a += 32) zs = fmax(zs, fabs(w.z[a]));
     zs = wmax(zs);
     const double tol = 1e-12 * zs;
     const int max_iter = 4 * n + 20;
+    if (GROUPS)
+        for (int k = lane; k < G; k += 32) w.nu[k] = 0.0;
     for (int it = 0; it < max_iter; ++it) {
         __syncwarp();
         int nF = 0;
@@ -348,7 +382,63 @@ __device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
             __syncwarp();
             for (int a = lane; a < nF; a += 32) w.y1[a] = w.r[a];
             tri_solve(w.A, w.iv, nF, w.y1, lane);
-            if (eq) {
+            if (GROUPS) {
+                for (int e = lane; e < nF * G; e += 32) {
+                    const int a = e % nF, k = e / nF;
+                    w.Y[e] = (w.F[a] % G == k) ? 1.0 : 0.0;
+                }
+                tri_solve_cols(w.A, w.iv, nF, w.Y, G, lane);
+                for (int e = lane; e < G * G; e += 32) {
+                    const int k = e % G, l = e / G;
+                    double s = 0.0;
+                    for (int a = 0; a < nF; ++a)
+                        if (w.F[a] % G == k) s += w.Y[a + nF * l];
+                    w.S[e] = s;
+                }
+                for (int k = lane; k < G; k += 32) {
+                    double s = 0.0;
+                    for (int a = 0; a < nF; ++a)
+                        if (w.F[a] % G == k) s += w.y1[a];
+                    for (int b = 0; b < n; ++b)
+                        if (w.st[b] != QF && b % G == k) s += w.d[b];
+                    w.rhs[k] = s;
+                }
+                __syncwarp();
+                if (lane == 0) {   // G x G Cholesky and the two sweeps, as the oracle
+                    double* S = w.S;
+                    double smax = 0.0;
+                    for (int k = 0; k < G; ++k) smax = fmax(smax, fabs(S[k + G * k]));
+                    const double sfl = 1e-300 + 1e-14 * smax;
+                    for (int c = 0; c < G; ++c) {
+                        double s = S[c + G * c];
+                        for (int k = 0; k < c; ++k) s -= S[c + G * k] * S[c + G * k];
+                        if (!(s > sfl)) s = sfl;
+                        const double lcc = sqrt(s);
+                        S[c + G * c] = lcc;
+                        for (int rr = c + 1; rr < G; ++rr) {
+                            double t = S[rr + G * c];
+                            for (int k = 0; k < c; ++k) t -= S[rr + G * k] * S[c + G * k];
+                            S[rr + G * c] = t / lcc;
+                        }
+                    }
+                    for (int a = 0; a < G; ++a) {
+                        double t = w.rhs[a];
+                        for (int k = 0; k < a; ++k) t -= S[a + G * k] * w.nu[k];
+                        w.nu[a] = t / S[a + G * a];
+                    }
+                    for (int a = G - 1; a >= 0; --a) {
+                        double t = w.nu[a];
+                        for (int k = a + 1; k < G; ++k) t -= S[k + G * a] * w.nu[k];
+                        w.nu[a] = t / S[a + G * a];
+                    }
+                }
+                __syncwarp();
+                for (int a = lane; a < nF; a += 32) {
+                    double t = w.y1[a];
+                    for (int l = 0; l < G; ++l) t -= w.Y[a + nF * l] * w.nu[l];
+                    w.ds[a] = t;
+                }
+            } else if (G == 1) {
                 for (int a = lane; a < nF; a += 32) w.y2[a] = 1.0;
                 tri_solve(w.A, w.iv, nF, w.y2, lane);
                 double cf = 0.0;
@@ -371,6 +461,11 @@ __device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
         int bidx = INT_MAX, bto = QF;
         for (int a = lane; a < nF; a += 32) {
             const int fa = w.F[a];
+            if (GROUPS) {   // a group's last free variable is fixed by its equality
+                int cnt = 0;
+                for (int b = 0; b < nF; ++b) cnt += (w.F[b] % G == fa % G);
+                if (cnt == 1) continue;
+            }
             const double s = w.ds[a] - w.d[fa];
             double ra = 2.0;
             int to = QF;
@@ -390,7 +485,7 @@ __device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
             for (int a = lane; a < n; a += 32) {
                 double s = -w.z[a];
                 for (int b = 0; b < n; ++b) s += H(a, b) * w.d[b];
-                w.g[a] = s + nu;
+                w.g[a] = s + (GROUPS ? w.nu[a % G] : nu);
             }
             __syncwarp();
             double wv = tol;
@@ -428,18 +523,23 @@ __device__ int warp_qp(int n, bool eq, const HF& H, const QPWork& w) {
 
 constexpr int QP_WARPS = 4;
 
-__device__ QPWork carve(double* base, int nmax) {
+// Per-warp workspace for problems of up to nmax variables and gmax >= 2
+// equality groups (gmax = 0 when the problems have at most one equality).
+__device__ QPWork carve(double* base, int nmax, int gmax = 0) {
     QPWork w;
     w.A = base;
     double* v = base + nmax * nmax;
     w.d = v; w.z = v + nmax; w.lo = v + 2 * nmax; w.hi = v + 3 * nmax; w.r = v + 4 * nmax;
     w.y1 = v + 5 * nmax; w.y2 = v + 6 * nmax; w.ds = v + 7 * nmax; w.g = v + 8 * nmax; w.iv = v + 9 * nmax;
-    w.st = reinterpret_cast<int*>(v + 10 * nmax);
+    double* e = v + 10 * nmax;
+    w.Y = e; w.S = e + nmax * gmax; w.nu = w.S + gmax * gmax; w.rhs = w.nu + gmax;
+    w.st = reinterpret_cast<int*>(w.rhs + gmax);
     w.F = w.st + nmax;
     return w;
 }
-__host__ __device__ constexpr size_t qp_warp_bytes(int nmax) {
-    return (size_t)(nmax * nmax + 10 * nmax) * sizeof(double) + (size_t)(2 * nmax) * sizeof(int);
+__host__ __device__ constexpr size_t qp_warp_bytes(int nmax, int gmax = 0) {
+    return (size_t)(nmax * nmax + 10 * nmax + nmax * gmax + gmax * gmax + 2 * gmax) * sizeof(double) +
+           (size_t)(2 * nmax) * sizeof(int);
 }
 
 struct HQ {
@@ -476,21 +576,28 @@ k_qp_q(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
     }
     __syncwarp();
     HQ H{XtX + (int64_t)K * K * pidx, K, pen_rho >= 0.0 ? pen_rho : 0.0};
-    const int it = warp_qp(K, pen_rho < 0.0, H, w);
+    const int it = warp_qp<false>(K, pen_rho < 0.0 ? 1 : 0, H, w);
     __syncwarp();
     for (int a = lane; a < K; a += 32) qdiff[(int64_t)K * pidx + a] = w.d[a];
     if (it < 0 && lane == 0) atomicAdd(slots + S_QP_FAIL, 1.0);
 }
 
+// G = 0: penalty form (rho, warm-started working set); G >= 1: equality form
+// with G = K groups (no rho, cold start: a warm-started working set would
+// break the equalities); GROUPS when G >= 2.
+template <bool GROUPS>
 __global__ void __launch_bounds__(32 * QP_WARPS)
 k_qp_p(int K, int64_t n, const double* __restrict__ XtX, const double* __restrict__ Xtz,
-       const double* __restrict__ p, double rho, double* __restrict__ pdiff, double* slots, int8_t* __restrict__ ws) {
+       const double* __restrict__ p, double rho, double* __restrict__ pdiff, double* slots, int8_t* __restrict__ ws,
+       int G) {
     extern __shared__ double smem_qp[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t j = (int64_t)blockIdx.x * QP_WARPS + warp;
     if (j >= n) return;
     const int nv = 4 * K;
-    QPWork w = carve(smem_qp + warp * (qp_warp_bytes(nv) / sizeof(double)), nv);
+    const int gmax = GROUPS ? G : 0;
+    if (G > 0) ws = nullptr;
+    QPWork w = carve(smem_qp + warp * (qp_warp_bytes(nv, gmax) / sizeof(double)), nv, gmax);
     for (int a = lane; a < nv; a += 32) {
         const double pa = p[(int64_t)nv * j + a];
         w.d[a] = 0.0;
@@ -504,8 +611,8 @@ k_qp_p(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
         w.d[a] = s0 == QL ? w.lo[a] : (s0 == QH ? w.hi[a] : 0.0);
     }
     __syncwarp();
-    HP H{XtX + (int64_t)K * K * 4 * j, K, rho};
-    const int it = warp_qp(nv, false, H, w);
+    HP H{XtX + (int64_t)K * K * 4 * j, K, G > 0 ? 0.0 : rho};
+    const int it = warp_qp<GROUPS>(nv, G, H, w);
     __syncwarp();
     for (int a = lane; a < nv; a += 32) {
         pdiff[(int64_t)nv * j + a] = w.d[a];
@@ -724,8 +831,11 @@ cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st) 
     return cudaGetLastError();
 }
 cudaError_t init_kernel_attrs() {
-    return cudaFuncSetAttribute(k_qp_p, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(QP_WARPS * qp_warp_bytes(4 * HX_KMAX)));
+    cudaError_t e = cudaFuncSetAttribute(k_qp_p<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(QP_WARPS * qp_warp_bytes(4 * HX_KMAX)));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_qp_p<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(QP_WARPS * qp_warp_bytes(4 * HX_KMAX, HX_KMAX)));
 }
 cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff,
                         double* slots, cudaStream_t st, double pen_rho) {
@@ -734,9 +844,14 @@ cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, 
     return cudaGetLastError();
 }
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
-                        double* pdiff, double* slots, int8_t* ws, cudaStream_t st) {
-    const size_t smem = QP_WARPS * qp_warp_bytes(4 * K);
-    k_qp_p<<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, p, rho, pdiff, slots, ws);
+                        double* pdiff, double* slots, int8_t* ws, cudaStream_t st, bool eq) {
+    const bool groups = eq && K >= 2;
+    const size_t smem = QP_WARPS * qp_warp_bytes(4 * K, groups ? K : 0);
+    if (groups)
+        k_qp_p<true><<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, p, rho, pdiff, slots, ws, K);
+    else
+        k_qp_p<false><<<nblk(n, QP_WARPS), 32 * QP_WARPS, smem, st>>>(K, n, XtX, Xtz, p, rho, pdiff, slots, ws,
+                                                                      eq ? 1 : 0);
     return cudaGetLastError();
 }
 int qn_dots_blocks(int64_t n) {

@@ -87,8 +87,9 @@ cudaError_t launch_step_p(const double* p, const double* d, int K, int64_t J, do
 cudaError_t init_kernel_attrs();
 cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff,
                         double* slots, cudaStream_t st, double pen_rho = -1.0);
+// eq: the equality form (K equalities per block, rho and ws unused)
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
-                        double* pdiff, double* slots, int8_t* ws, cudaStream_t st);
+                        double* pdiff, double* slots, int8_t* ws, cudaStream_t st, bool eq = false);
 // ZAL quasi-Newton
 int qn_dots_blocks(int64_t n);
 cudaError_t launch_qn(int64_t n, const double* x, const double* xn, const double* xn2, double* U, double* V,

@@ -174,7 +174,8 @@ class GB300Admix:
 
     def set_loop_opts(self, fix_q=False, fix_p=False, guarantee_increase=False, penalty=None):
         """admixture_qn!/init_em! keyword options (src/algorithms_outer.jl:1-3, 38-41);
-        penalty None is the reference default, True the penalty form for both steps."""
+        penalty None is the reference default (P penalty form, Q equality form),
+        True the penalty form for both steps, False the equality form for both."""
         o = _lib.HxLoopOpts()
         self._ck(self.lib.hx_loop_opts_default(C.byref(o)))
         o.fix_q, o.fix_p, o.guarantee_increase = int(fix_q), int(fix_p), int(guarantee_increase)

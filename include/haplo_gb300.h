@@ -88,7 +88,8 @@ typedef struct hx_loop_opts {
                                     (src/algorithms_inner.jl:169-199 Q with >=, :313-343 P with >) */
     int32_t penalty;             /* -1 (default, penalty=nothing): P penalty form, Q equality form;
                                     1: penalty form for both (rho * 1 1' on each Q block);
-                                    0: equality forms for both -> HX_EUNSUPPORTED (P equality form not built) */
+                                    0: equality form for both (P: sum_h d[k,h] = 0 for every k,
+                                       src/algorithms_inner.jl:307-310) */
 } hx_loop_opts;
 
 /* Defaults: precision FP64, device 0, Qsec 3, rho 1e7, pseudocount 1e-5. */
@@ -137,10 +138,12 @@ int hx_update_p_accum(hx_ctx* ctx, const double* q, const double* p, double* XtX
 
 /* ---- batched QP / projection (CPU-only in the reference) on host arrays ---- */
 /* Per individual: argmin 0.5 d'Hd - g'd, sum d = 0, 0 <= q+d <= 1 with
- * H = XtX[:,:,i], g = Xtz[:,i] (algorithms_inner.jl:134-168). n individuals. */
+ * H = XtX[:,:,i], g = Xtz[:,i] (algorithms_inner.jl:134-168). n individuals.
+ * With loop option penalty = 1: H + rho 1 1' and no equality (:158-162). */
 int hx_qp_q(hx_ctx* ctx, int64_t n, const double* XtX, const double* Xtz, const double* q, double* qdiff);
 /* Per block: 4K variables, H = blockdiag(XtX[:,:,4j+h]) + rho on the
- * (h,h2,k) pattern, 0 <= p+d <= 1 (algorithms_inner.jl:264-305). n blocks. */
+ * (h,h2,k) pattern, 0 <= p+d <= 1 (algorithms_inner.jl:264-305). n blocks.
+ * With loop option penalty = 0: no rho and sum_h d[k,h] = 0 for every k (:307-310). */
 int hx_qp_p(hx_ctx* ctx, int64_t n, const double* XtX, const double* Xtz, const double* p, double* pdiff);
 /* OpenADMIXTURE.project_q! per column / project_p! per (k, block) quartet. */
 int hx_project_q(hx_ctx* ctx, int64_t ncol, double* q);

@@ -218,19 +218,29 @@ void project_simplex(double* v, int n, int64_t st, double eps) {
 }
 
 // ---------------------------------------------------------------- QP
-// Exact minimiser of 0.5 d'Hd - z'd subject to lo <= d <= hi and, when eq,
-// sum(d) = 0.  Primal active-set method; H is n x n column-major, SPD on the
+// Exact minimiser of 0.5 d'Hd - z'd subject to lo <= d <= hi and ngrp
+// equality groups: ngrp = 0, none; ngrp = 1, sum(d) = 0; ngrp = G >= 2,
+// sum over {a : a % G == k} of d_a = 0 for every k < G.  Primal active-set
+// method from the feasible start d = 0; H is n x n column-major, SPD on the
 // subspaces visited.  This restates the contract of OpenADMIXTURE's
 // create_tableau!/quadratic_program! pair as used at
-// src/algorithms_inner.jl:160-166 (K variables, one equality) and :303-305
-// (4K variables, penalty form, no equality).  Returns iterations used, or -1
-// when the iteration cap was hit (d is then the last feasible iterate).
+// src/algorithms_inner.jl:160-166 (K variables, one equality), :303-305
+// (4K variables, penalty form, no equality) and :307-310 (4K variables, K
+// equalities: the P quartets of each ancestry sum to zero, variable h*K + k
+// in group k).  With G >= 2 groups the multipliers solve the G x G Schur
+// system S nu = E_F H_FF^-1 r + E_X d_X with S = E_F H_FF^-1 E_F'; a group's
+// last free variable is determined by its equality and never blocks the
+// ratio test, so every group keeps a free variable and S stays definite.
+// Returns iterations used, or -1 when the iteration cap was hit (d is then
+// the last feasible iterate).
 int qp_active_set(int n, const double* H, const double* z, const double* lo, const double* hi,
-                  bool eq, double* d) {
+                  int ngrp, double* d) {
     enum { FREE = 0, AT_LO = 1, AT_HI = 2 };
+    const int G = ngrp;
     std::vector<int> st(n, FREE);
     std::vector<double> A(n * n), r(n), y1(n), y2(n), g(n);
-    std::vector<int> F(n);
+    std::vector<double> Y((size_t)n * std::max(G, 1)), S((size_t)G * G), nug(std::max(G, 1), 0.0);
+    std::vector<int> F(n), nfree(std::max(G, 1));
     for (int a = 0; a < n; ++a) {
         d[a] = 0.0;
         if (lo[a] >= 0.0 && hi[a] <= 0.0) st[a] = AT_LO;  // degenerate box: pinned at 0
@@ -283,7 +293,55 @@ int qp_active_set(int n, const double* H, const double* z, const double* lo, con
             };
             for (int a = 0; a < nF; ++a) y1[a] = r[a];
             solve(y1);
-            if (eq) {
+            if (G >= 2) {
+                // Y = H_FF^-1 E_F' (column k: indicator of group k), S = E_F Y
+                for (int k = 0; k < G; ++k) {
+                    for (int a = 0; a < nF; ++a) y2[a] = (F[a] % G == k) ? 1.0 : 0.0;
+                    solve(y2);
+                    for (int a = 0; a < nF; ++a) Y[a + (size_t)nF * k] = y2[a];
+                }
+                std::vector<double> rhs(G, 0.0);
+                for (int k = 0; k < G; ++k)
+                    for (int l = 0; l < G; ++l) S[k + G * l] = 0.0;
+                for (int a = 0; a < nF; ++a) {
+                    const int k = F[a] % G;
+                    rhs[k] += y1[a];
+                    for (int l = 0; l < G; ++l) S[k + G * l] += Y[a + (size_t)nF * l];
+                }
+                for (int b = 0; b < n; ++b)
+                    if (st[b] != FREE) rhs[b % G] += d[b];
+                // Cholesky of the G x G Schur complement, then S nu = rhs
+                double smax = 0.0;
+                for (int k = 0; k < G; ++k) smax = std::max(smax, std::fabs(S[k + G * k]));
+                const double sfl = 1e-300 + 1e-14 * smax;
+                for (int c = 0; c < G; ++c) {
+                    double s = S[c + G * c];
+                    for (int k = 0; k < c; ++k) s -= S[c + G * k] * S[c + G * k];
+                    if (!(s > sfl)) s = sfl;
+                    const double lcc = std::sqrt(s);
+                    S[c + G * c] = lcc;
+                    for (int rr = c + 1; rr < G; ++rr) {
+                        double t = S[rr + G * c];
+                        for (int k = 0; k < c; ++k) t -= S[rr + G * k] * S[c + G * k];
+                        S[rr + G * c] = t / lcc;
+                    }
+                }
+                for (int a = 0; a < G; ++a) {
+                    double t = rhs[a];
+                    for (int k = 0; k < a; ++k) t -= S[a + G * k] * nug[k];
+                    nug[a] = t / S[a + G * a];
+                }
+                for (int a = G - 1; a >= 0; --a) {
+                    double t = nug[a];
+                    for (int k = a + 1; k < G; ++k) t -= S[k + G * a] * nug[k];
+                    nug[a] = t / S[a + G * a];
+                }
+                for (int a = 0; a < nF; ++a) {
+                    double t = y1[a];
+                    for (int l = 0; l < G; ++l) t -= Y[a + (size_t)nF * l] * nug[l];
+                    dstar[a] = t;
+                }
+            } else if (G == 1) {
                 for (int a = 0; a < nF; ++a) y2[a] = 1.0;
                 solve(y2);
                 double cfix = 0.0;
@@ -299,8 +357,13 @@ int qp_active_set(int n, const double* H, const double* z, const double* lo, con
         // ratio test along s = dstar - d_F
         double alpha = 1.0;
         int blk = -1, blk_to = FREE;
+        if (G >= 2) {
+            for (int k = 0; k < G; ++k) nfree[k] = 0;
+            for (int a = 0; a < nF; ++a) nfree[F[a] % G]++;
+        }
         for (int a = 0; a < nF; ++a) {
             int fa = F[a];
+            if (G >= 2 && nfree[fa % G] == 1) continue;   // fixed by its group's equality
             double s = dstar[a] - d[fa];
             if (s < 0.0) {
                 double ra = (lo[fa] - d[fa]) / s;
@@ -316,7 +379,7 @@ int qp_active_set(int n, const double* H, const double* z, const double* lo, con
             for (int a = 0; a < n; ++a) {
                 double s = -z[a];
                 for (int b = 0; b < n; ++b) s += H[a + (int64_t)n * b] * d[b];
-                g[a] = s + nu;
+                g[a] = s + (G >= 2 ? nug[a % G] : nu);
             }
             int rel = -1;
             double worst = tol;
@@ -516,11 +579,12 @@ int qp_q_batch(int K, int64_t I, const double* XtX, const double* Xtz, const dou
     return fails.load();
 }
 
-// src/algorithms_inner.jl:264-305 (penalty branch, the default): block-diagonal
-// 4K x 4K Hessian (274-283), + rho on the (l,l2,k) pattern (295-302).
-// Variable v = h*K + k <-> p[k, 4j+h].
+// src/algorithms_inner.jl:264-310: block-diagonal 4K x 4K Hessian (274-283).
+// eq = 0: the penalty branch (the default), + rho on the (l,l2,k) pattern
+// (295-305).  eq = 1: the equality branch (307-310), no penalty and the K
+// equalities sum_h d[k, h] = 0.  Variable v = h*K + k <-> p[k, 4j+h].
 int qp_p_batch(int K, int64_t J, const double* XtX, const double* Xtz, const double* p, double rho,
-               double* pdiff, int nthreads) {
+               double* pdiff, int nthreads, int eq = 0) {
     std::atomic<int> fails(0);
     const int n = 4 * K;
     parallel_for(J, nthreads, [&](int64_t a, int64_t b) {
@@ -531,12 +595,13 @@ int qp_p_batch(int K, int64_t J, const double* XtX, const double* Xtz, const dou
                 for (int k = 0; k < K; ++k)
                     for (int k2 = 0; k2 < K; ++k2)
                         H[(l * K + k2) + n * (l * K + k)] = XtX[(int64_t)K * K * (4 * j + l) + k2 + K * k];
-            for (int l2 = 0; l2 < 4; ++l2)
-                for (int l = 0; l < 4; ++l)
-                    for (int k = 0; k < K; ++k) H[(l * K + k) + n * (l2 * K + k)] += rho;
+            if (!eq)
+                for (int l2 = 0; l2 < 4; ++l2)
+                    for (int l = 0; l < 4; ++l)
+                        for (int k = 0; k < K; ++k) H[(l * K + k) + n * (l2 * K + k)] += rho;
             const double* pj = p + (int64_t)n * j;
             for (int v = 0; v < n; ++v) { lo[v] = 0.0 - pj[v]; hi[v] = 1.0 - pj[v]; }
-            int it = qp_active_set(n, H.data(), Xtz + (int64_t)n * j, lo.data(), hi.data(), false,
+            int it = qp_active_set(n, H.data(), Xtz + (int64_t)n * j, lo.data(), hi.data(), eq ? K : 0,
                                    pdiff + (int64_t)n * j);
             if (it < 0) fails++;
         }
@@ -638,7 +703,7 @@ void orc_project_q(double* q, int K, int64_t ncol, double eps) { project_q_all(q
 void orc_project_p(double* p, int K, int64_t J, double eps) { project_p_all(p, K, J, eps, 1); }
 
 int orc_qp_dense(int n, const double* H, const double* z, const double* lo, const double* hi, int eq, double* d) {
-    return qp_active_set(n, H, z, lo, hi, eq != 0, d);
+    return qp_active_set(n, H, z, lo, hi, eq, d);
 }
 int orc_qp_q(int K, int64_t I, const double* XtX, const double* Xtz, const double* q, double* qdiff, int nthreads) {
     return qp_q_batch(K, I, XtX, Xtz, q, qdiff, nthreads);
@@ -646,6 +711,10 @@ int orc_qp_q(int K, int64_t I, const double* XtX, const double* Xtz, const doubl
 int orc_qp_p(int K, int64_t J, const double* XtX, const double* Xtz, const double* p, double rho, double* pdiff,
              int nthreads) {
     return qp_p_batch(K, J, XtX, Xtz, p, rho, pdiff, nthreads);
+}
+int orc_qp_p_eq(int K, int64_t J, const double* XtX, const double* Xtz, const double* p, double* pdiff,
+                int nthreads) {
+    return qp_p_batch(K, J, XtX, Xtz, p, 0.0, pdiff, nthreads, 1);
 }
 
 // src/algorithms_inner.jl:29-84 (em!, CPU branch): q_next ./= 2(J - dm);
@@ -731,8 +800,8 @@ void orc_zal(int64_t n, const double* x, const double* x_next, const double* x_n
 // fix_q / fix_p keep Q or P; guarantee_increase halves each update's step
 // until the log-likelihood does not drop (src/algorithms_inner.jl:169-199 for
 // Q with >=, :313-343 for P with >); penalty -1 is the default (P penalty
-// form, Q equality form), 1 the penalty form for both.  The P equality form
-// (penalty 0) is not restated.
+// form, Q equality form), 1 the penalty form for both, 0 the equality form
+// for both (src/algorithms_outer.jl:58-64).
 struct LoopOpts {
     int fix_q = 0, fix_p = 0, gi = 0, penalty = -1;
 };
@@ -766,7 +835,7 @@ void update_p_opts(const Dims& D, const double* q, const double* p, double* p_ne
     if (o.fix_p) { std::memcpy(p_next, p, n * sizeof(double)); return; }
     std::vector<double> XtX((size_t)K * K * 4 * D.J), Xtz((size_t)n), pd((size_t)n);
     accum_p(D, q, p, XtX.data(), Xtz.data(), nthreads);
-    qp_p_batch(K, D.J, XtX.data(), Xtz.data(), p, rho, pd.data(), nthreads);
+    qp_p_batch(K, D.J, XtX.data(), Xtz.data(), p, rho, pd.data(), nthreads, o.penalty == 0);
     double factor = 1.0;
     for (;;) {
         for (int64_t a = 0; a < n; ++a) p_next[a] = p[a] + factor * pd[a];
@@ -787,13 +856,12 @@ void update_p_opts(const Dims& D, const double* q, const double* p, double* p_ne
 // receives ll after every outer iteration.  EM with fix_q / fix_p keeps that
 // factor unchanged (the reference's em! rescales a fixed q before projecting
 // it and rebinds p_next to p, algorithms_inner.jl:45-52, which is not
-// restated).  Returns 0, or -2 for the unsupported P equality form.
+// restated).  Returns 0.
 int orc_fit_ex(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J, int K, int Qs, double* x,
                int n_iter, double rtol, int em_iters, double rho, int nthreads, double* ll_out, int* iters_out,
                double* trace, int fix_q, int fix_p, int guarantee_increase, int penalty) {
     LoopOpts o;
     o.fix_q = fix_q; o.fix_p = fix_p; o.gi = guarantee_increase; o.penalty = penalty;
-    if (penalty == 0) return -2;
     Dims D{bed, bps, nsnp, I, J, K};
     const int64_t n = (int64_t)K * (I + 4 * J);
     std::vector<int64_t> dm(I);

@@ -45,6 +45,7 @@ def _load():
             "orc_qp_dense": (I32, [I32, P, P, P, P, I32, P]),
             "orc_qp_q": (I32, [I32, I64, P, P, P, P, I32]),
             "orc_qp_p": (I32, [I32, I64, P, P, P, Dd, P, I32]),
+            "orc_qp_p_eq": (I32, [I32, I64, P, P, P, P, I32]),
             "orc_em_step": (None, [P, I64, I64, I64, I32, P, P, P, P, P, I32]),
             "orc_update_q": (I32, [P, I64, I64, I64, I32, P, P, P, P, P, I32]),
             "orc_update_p": (I32, [P, I64, I64, I64, I32, P, P, Dd, P, P, P, I32]),
@@ -152,11 +153,13 @@ def project_p(p, eps=1e-5):
 
 
 def qp_dense(H, z, lo, hi, eq):
+    """eq: False/0 no equality, True/1 sum(d) = 0, G >= 2 the G groups
+    sum_{a % G == k} d_a = 0."""
     n = len(z)
     H = _F(H, (n, n))
     z, lo, hi = (np.ascontiguousarray(v, dtype=np.float64) for v in (z, lo, hi))
     d = np.zeros(n)
-    it = _load().orc_qp_dense(n, _p(H), _p(z), _p(lo), _p(hi), 1 if eq else 0, _p(d))
+    it = _load().orc_qp_dense(n, _p(H), _p(z), _p(lo), _p(hi), int(eq), _p(d))
     return d, it
 
 
@@ -173,6 +176,15 @@ def qp_p(XtX, Xtz, p, rho=1e7, threads=None):
     XtX, Xtz, p = _F(XtX, (K, K, m)), _F(Xtz, (K, m)), _F(p, (K, m))
     d = np.empty((K, m), order="F")
     f = _load().orc_qp_p(K, m // 4, _p(XtX), _p(Xtz), _p(p), rho, _p(d), threads or nthreads())
+    return d, f
+
+
+def qp_p_eq(XtX, Xtz, p, threads=None):
+    """The P QP in equality form (penalty = false): sum_h d[k, h] = 0 for every k."""
+    K, m = p.shape
+    XtX, Xtz, p = _F(XtX, (K, K, m)), _F(Xtz, (K, m)), _F(p, (K, m))
+    d = np.empty((K, m), order="F")
+    f = _load().orc_qp_p_eq(K, m // 4, _p(XtX), _p(Xtz), _p(p), _p(d), threads or nthreads())
     return d, f
 
 
@@ -214,7 +226,7 @@ def fit(b, K, q, p, n_iter=1000, rtol=1e-7, em_iters=5, Qs=3, rho=1e7, threads=N
         guarantee_increase=False, penalty=None):
     """init_em! + admixture_qn! on the CPU; returns (q, p, ll, iters, trace).
     penalty None is the reference default (P penalty form, Q equality form);
-    True uses the penalty form for both."""
+    True uses the penalty form for both, False the equality form for both."""
     q, p = _F(q, (K, b.I)), _F(p, (K, 4 * b.J))
     x = np.asfortranarray(np.hstack([q, p]))
     ll = C.c_double()
@@ -224,8 +236,6 @@ def fit(b, K, q, p, n_iter=1000, rtol=1e-7, em_iters=5, Qs=3, rho=1e7, threads=N
     r = _load().orc_fit_ex(b.ptr, b.bps, b.n_snp, b.I, b.J, K, Qs, _p(x), n_iter, rtol, em_iters, rho,
                            threads or nthreads(), C.byref(ll), C.byref(iters), _p(trace), int(fix_q), int(fix_p),
                            int(guarantee_increase), pen)
-    if r == -2:
-        raise NotImplementedError("the P equality form (penalty=False) is not restated")
     return (np.asfortranarray(x[:, :b.I]), np.asfortranarray(x[:, b.I:]), ll.value, iters.value,
             trace[:iters.value])
 

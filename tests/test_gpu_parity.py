@@ -196,7 +196,7 @@ def test_errors_are_status_codes(hx, coh):
 
 
 @pytest.mark.parametrize("opts", [dict(fix_q=True), dict(fix_p=True), dict(guarantee_increase=True),
-                                  dict(penalty=True)])
+                                  dict(penalty=True), dict(penalty=False)])
 def test_loop_options_match_oracle_fp64(hx, O, opts):
     # admixture_qn!/init_em! keywords (src/algorithms_outer.jl:1-3, 38-41)
     c = small_cohort(240, 120, 3, seed=33, alpha=0.5, miss=0.01)
@@ -218,8 +218,30 @@ def test_loop_options_match_oracle_fp64(hx, O, opts):
         np.testing.assert_allclose(pd, p0, rtol=0, atol=1e-15)
 
 
-def test_p_equality_form_is_reported_unsupported(hx, coh):
-    from haplo_gb300 import HxError
+@pytest.mark.parametrize("K", [2, 3, 5, 8, 12])
+def test_qp_p_equality_form_matches_oracle(hx, O, K):
+    # penalty = false: per block, 4K variables with the K equalities
+    # sum_h d[k, h] = 0 (src/algorithms_inner.jl:307-310)
+    c = small_cohort(300, 160, K, seed=40 + K, alpha=0.4, miss=0.01)
+    b = O.Bed(c["bed"], c["I"], c["J"])
+    q, p = start(c, seed=K)
+    XtX, Xtz = O.accum_p(b, K, q, p)
+    do, fails = O.qp_p_eq(XtX, Xtz, p)
+    assert fails == 0
+    d = make(hx, c)
+    d.set_loop_opts(penalty=False)
+    dg = d.qp_p(XtX, Xtz, p)
+    scale = np.abs(do).max()
+    assert np.abs(dg - do).max() <= 1e-9 * max(scale, 1.0)
+    np.testing.assert_allclose(dg.reshape(K, -1, 4).sum(axis=2), 0.0, atol=1e-12)
+
+
+def test_loop_opts_reject_unknown_penalty(hx, coh):
+    import ctypes as C
+    from haplo_gb300 import HxError, _lib
     d = make(hx, coh)
+    o = _lib.HxLoopOpts()
+    d._ck(d.lib.hx_loop_opts_default(C.byref(o)))
+    o.penalty = 2
     with pytest.raises(HxError):
-        d.set_loop_opts(penalty=False)
+        d._ck(d.lib.hx_set_loop_opts(d._h, C.byref(o)))

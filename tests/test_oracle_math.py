@@ -64,23 +64,31 @@ def test_em_step_increases_loglik(O, coh):
     np.testing.assert_allclose(p.reshape(K, -1, 4).sum(axis=2), 1.0, rtol=1e-12)
 
 
+def _groups(eq, n):
+    """Equality groups as index lists: eq False -> none, True -> one sum over
+    all variables, G >= 2 -> {a : a % G == k} for every k < G."""
+    G = 0 if eq is False else (1 if eq is True else int(eq))
+    return [[a for a in range(n) if a % G == k] for k in range(G)] if G else []
+
+
 def _kkt(H, z, lo, hi, eq, d, tol):
-    """KKT of min 0.5 d'Hd - z'd, lo <= d <= hi (, sum d = 0): with g = Hd - z
-    there is a multiplier nu (0 without the equality) such that g + nu >= 0 at
-    lower bounds, <= 0 at upper bounds and = 0 on free variables."""
+    """KKT of min 0.5 d'Hd - z'd, lo <= d <= hi and the equality groups of
+    `eq` (each group sums to 0): with g = Hd - z there is a multiplier nu per
+    group (0 off the groups) such that g + nu >= 0 at lower bounds, <= 0 at
+    upper bounds and = 0 on free variables."""
+    n = len(d)
     g = H @ d - z
     assert np.all(d >= lo - 1e-12) and np.all(d <= hi + 1e-12)
     at_lo = d <= lo + 1e-12
     at_hi = (d >= hi - 1e-12) & ~at_lo
     free = ~at_lo & ~at_hi
-    if eq:
-        assert abs(d.sum()) < 1e-10
-        nu_min = max([-g[a] for a in range(len(d)) if at_lo[a] or free[a]], default=-np.inf)
-        nu_max = min([-g[a] for a in range(len(d)) if at_hi[a] or free[a]], default=np.inf)
+    nu = np.zeros(n)
+    for grp in _groups(eq, n):
+        assert abs(d[grp].sum()) < 1e-10
+        nu_min = max([-g[a] for a in grp if at_lo[a] or free[a]], default=-np.inf)
+        nu_max = min([-g[a] for a in grp if at_hi[a] or free[a]], default=np.inf)
         assert nu_min <= nu_max + 2 * tol
-        nu = nu_max if np.isfinite(nu_max) else nu_min
-    else:
-        nu = 0.0
+        nu[grp] = nu_max if np.isfinite(nu_max) else nu_min
     r = g + nu
     assert np.all(r[at_lo] >= -2 * tol)
     assert np.all(r[at_hi] <= 2 * tol)
@@ -90,6 +98,7 @@ def _kkt(H, z, lo, hi, eq, d, tol):
 def _brute(H, z, lo, hi, eq):
     """Minimum over all assignments of variables to {lo, hi, free}."""
     n = len(z)
+    grps = _groups(eq, n)
     best, bd = np.inf, None
     for assign in itertools.product((0, 1, 2), repeat=n):
         fixed = [a for a in range(n) if assign[a] != 2]
@@ -100,22 +109,27 @@ def _brute(H, z, lo, hi, eq):
         if free:
             Hf = H[np.ix_(free, free)]
             r = z[free] - H[np.ix_(free, fixed)] @ d[fixed] if fixed else z[free]
-            if eq:
-                m = len(free)
-                KKT = np.zeros((m + 1, m + 1))
-                KKT[:m, :m] = Hf
-                KKT[:m, m] = 1
-                KKT[m, :m] = 1
-                rhs = np.concatenate([r, [-d[fixed].sum()]])
+            E = np.array([[1.0 if a in grp else 0.0 for a in free] for grp in grps]).reshape(len(grps), len(free))
+            keep = [e for e in range(len(grps)) if E[e].any()]
+            if any(abs(d[grps[e]].sum()) > 1e-12 for e in range(len(grps)) if e not in keep):
+                continue
+            E = E[keep]
+            m, c = len(free), len(keep)
+            KKT = np.zeros((m + c, m + c))
+            KKT[:m, :m] = Hf
+            KKT[:m, m:] = E.T
+            KKT[m:, :m] = E
+            rhs = np.concatenate([r, [-d[[a for a in grps[e] if a in fixed]].sum() for e in keep]])
+            try:
                 sol = np.linalg.solve(KKT, rhs)
-                d[free] = sol[:m]
-            else:
-                d[free] = np.linalg.solve(Hf, r)
-        elif eq and abs(d.sum()) > 1e-12:
+            except np.linalg.LinAlgError:
+                continue
+            d[free] = sol[:m]
+        elif any(abs(d[grp].sum()) > 1e-12 for grp in grps):
             continue
         if np.any(d < lo - 1e-12) or np.any(d > hi + 1e-12):
             continue
-        if eq and abs(d.sum()) > 1e-9:
+        if any(abs(d[grp].sum()) > 1e-9 for grp in grps):
             continue
         f = 0.5 * d @ H @ d - z @ d
         if f < best:
@@ -140,6 +154,44 @@ def test_qp_matches_brute_force(O, seed, eq):
     assert f == pytest.approx(best, rel=1e-9, abs=1e-9)
     np.testing.assert_allclose(d, bd, atol=1e-8)
     _kkt(H, z, lo, hi, eq, d, 1e-8 * (1 + np.abs(z).max()))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_qp_groups_match_brute_force(O, seed):
+    # the P equality form: 4K variables h*K + k, group k sums to zero (K = 2)
+    rng = np.random.default_rng(100 + seed)
+    K, n = 2, 8
+    H = np.zeros((n, n))
+    for l in range(4):
+        A = rng.normal(size=(K, K))
+        H[l * K:(l + 1) * K, l * K:(l + 1) * K] = A @ A.T + 0.1 * np.eye(K)
+    z = rng.normal(size=n) * 3
+    x = np.concatenate([rng.dirichlet(np.ones(4)) for _ in range(K)]).reshape(K, 4).T.ravel()
+    lo, hi = -x, 1 - x
+    d, it = O.qp_dense(H, z, lo, hi, K)
+    assert it > 0
+    bd, best = _brute(H, z, lo, hi, K)
+    f = 0.5 * d @ H @ d - z @ d
+    assert f == pytest.approx(best, rel=1e-9, abs=1e-9)
+    np.testing.assert_allclose(d, bd, atol=1e-8)
+    _kkt(H, z, lo, hi, K, d, 1e-8 * (1 + np.abs(z).max()))
+
+
+def test_qp_p_equality_form_satisfies_kkt(O, coh):
+    b, K, q, p = coh["b"], coh["K"], coh["q0"], coh["p0"]
+    XtXp, Xtzp = O.accum_p(b, K, q, p)
+    dp, fails = O.qp_p_eq(XtXp, Xtzp, p)
+    assert fails == 0
+    n = 4 * K
+    np.testing.assert_allclose(dp.reshape(K, -1, 4).sum(axis=2), 0.0, atol=1e-12)
+    for j in range(0, coh["J"], 5):
+        H = np.zeros((n, n))
+        for l in range(4):
+            H[l * K:(l + 1) * K, l * K:(l + 1) * K] = XtXp[:, :, 4 * j + l]
+        z = Xtzp[:, 4 * j:4 * j + 4].ravel(order="F")
+        pj = p[:, 4 * j:4 * j + 4].ravel(order="F")
+        dj = dp[:, 4 * j:4 * j + 4].ravel(order="F")
+        _kkt(H, z, -pj, 1 - pj, K, dj, 1e-7 * (1 + np.abs(z).max()))
 
 
 def test_qp_batches_satisfy_kkt(O, coh):
@@ -270,5 +322,5 @@ def test_penalty_true_fit_matches_default_optimum(O, loop_case):
     _, _, ll_pen, _, _ = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3, penalty=True)
     _, _, ll_def, _, _ = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3)
     assert ll_pen == pytest.approx(ll_def, rel=1e-6)
-    with pytest.raises(NotImplementedError):
-        O.fit(b, 3, q0, p0, n_iter=2, penalty=False)
+    _, _, ll_eq, _, _ = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3, penalty=False)
+    assert ll_eq == pytest.approx(ll_def, rel=1e-6)
