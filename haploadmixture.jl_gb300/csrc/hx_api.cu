@@ -43,6 +43,7 @@ struct hx_ctx {
     double ll_tmp = NAN;         // d.ll_tmp of the step control
     bool shared_geno = false;    // G and dm belong to the parent context (hx_create_shared)
     int S_q = 1, wpc_q = 1, S_p = 1, ipc_p = 1;
+    int S_ll = 1, wpc_ll = 1;                // FP32 log-likelihood pass
     bool tc = false;                         // Hessian passes on the tensor cores
     int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
     bool have_qp = false;
@@ -123,7 +124,28 @@ void prof_resolve(hx_ctx* c) {
 inline double* qof(double* x) { return x; }
 inline double* pof(hx_ctx* c, double* x) { return x + (int64_t)c->K * c->I; }
 
+// Chunks per tile for a pass of `tiles` independent tiles, each splitting
+// `units` (word columns or 32-individual stages) into chunks, on `slots`
+// resident CTAs: at least `waves` waves, and among up to twice that many
+// chunks the count whose last wave is fullest (a part-filled last wave idles
+// SMs for a whole CTA lifetime).  Returns the chunk length in units.
+int64_t pick_chunk(int64_t tiles, int64_t units, int64_t slots, int64_t waves) {
+    const int64_t s0 = std::min(units, std::max<int64_t>(1, (waves * slots + tiles - 1) / tiles));
+    int64_t best = (units + s0 - 1) / s0;
+    double beff = -1.0;
+    for (int64_t s = s0; s <= std::min(units, 2 * s0); ++s) {
+        const int64_t per = (units + s - 1) / s;
+        const int64_t sa = (units + per - 1) / per;            // chunks formed
+        const double w = (double)(tiles * sa) / (double)slots;
+        const double eff = w / std::ceil(w);
+        if (eff > beff + 1e-9) { beff = eff; best = per; }
+    }
+    return best;
+}
+
 void plan(hx_ctx* c) {
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
     const int64_t target = 2048;
     const int64_t tilesQ = c->Ipad / ACC_THREADS;
     int64_t S = std::max<int64_t>(1, (target + tilesQ - 1) / tilesQ);
@@ -137,19 +159,18 @@ void plan(hx_ctx* c) {
     ipc = (ipc + PSTAGE_IND - 1) / PSTAGE_IND * PSTAGE_IND;
     c->ipc_p = (int)ipc;
     c->S_p = (int)((c->I + ipc - 1) / ipc);
-    // tensor-core passes: two 256-thread CTAs per SM; aim for >= 8 waves of 2 x 152
-    const int64_t target_tc = 8 * 2 * 152;
-    int64_t St = std::max<int64_t>(1, (target_tc + tilesQ - 1) / tilesQ);
-    St = std::min<int64_t>(St, c->JW);
-    int64_t wpc = (c->JW + St - 1) / St;     // stages of one word (8 blocks)
+    // tensor-core passes (stages of one word column, Q, or 32 individuals, P)
+    // and the FP32 log-likelihood pass: >= 8 waves with a full last wave
+    const int64_t wpc = pick_chunk(tilesQ, c->JW, (int64_t)nsm * tc_resident(c->K, false), 8);
     c->wpc_qt = (int)wpc;
     c->S_qt = (int)((c->JW + wpc - 1) / wpc);
-    int64_t Spt = std::max<int64_t>(1, (target_tc + tilesP - 1) / tilesP);
-    Spt = std::min<int64_t>(Spt, (c->I + 31) / 32);
-    int64_t ipt = (c->I + Spt - 1) / Spt;
-    ipt = (ipt + 31) / 32 * 32;              // whole stages of 32 individuals
-    c->ipc_pt = (int)ipt;
-    c->S_pt = (int)((c->I + ipt - 1) / ipt);
+    const int64_t nst = (c->I + 31) / 32;
+    const int64_t spc = pick_chunk(tilesP, nst, (int64_t)nsm * tc_resident(c->K, true), 8);
+    c->ipc_pt = (int)(spc * 32);
+    c->S_pt = (int)((nst + spc - 1) / spc);
+    const int64_t tilesL = loglik_f32x2_blocks(c->Ipad, c->K);
+    c->wpc_ll = (int)pick_chunk(tilesL, c->JW, (int64_t)nsm * loglik_f32x2_resident(c->K), 8);
+    c->S_ll = (c->JW + c->wpc_ll - 1) / c->wpc_ll;
 }
 
 PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
@@ -207,9 +228,10 @@ int loglik_to_slot(hx_ctx* c, const double* q, const double* p, int slot) {
         HX_LAUNCH(HX_KIND_OTHER, 1,
                   launch_reduce_sum(c->part_ll, (c->Ipad / ACC_THREADS) * c->S_q, c->slots + slot, c->st));
     } else {
+        a.S = c->S_ll; a.per_chunk = c->wpc_ll;
         HX_LAUNCH(HX_KIND_LOGLIK, 1, launch_loglik_f32x2(c->K, a, c->st));
         HX_LAUNCH(HX_KIND_OTHER, 1,
-                  launch_reduce_sum(c->part_ll, (int64_t)loglik_f32x2_blocks(c->Ipad, c->K) * c->S_q, c->slots + slot,
+                  launch_reduce_sum(c->part_ll, (int64_t)loglik_f32x2_blocks(c->Ipad, c->K) * c->S_ll, c->slots + slot,
                                     c->st));
     }
     return HX_OK;
@@ -381,6 +403,12 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_CK(init_kernel_attrs());
     HX_CK(init_tc_attrs());
     plan(c);
+    if (c->verbose)
+        fprintf(stderr,
+                "{\"plan\": {\"chunks_q\": %d, \"chunks_p\": %d, \"chunks_q_tc\": %d, \"chunks_p_tc\": %d, "
+                "\"chunks_loglik\": %d, \"resident_q_tc\": %d, \"resident_p_tc\": %d, \"resident_loglik\": %d}}\n",
+                c->S_q, c->S_p, c->S_qt, c->S_pt, c->S_ll, tc_resident(K, false), tc_resident(K, true),
+                loglik_f32x2_resident(K));
     const int NVmax = K + K * (K + 1) / 2;
     if (parent) {
         c->G = parent->G;
@@ -400,7 +428,8 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_ST(dalloc(c, &c->part_q, (size_t)std::max(c->S_q, c->tc ? c->S_qt : 1) * NVmax * c->Ipad));
     const int Sp_max = std::max(c->S_p, c->tc ? c->S_pt : 1);
     if (Sp_max > 1) HX_ST(dalloc(c, &c->part_p, (size_t)Sp_max * NVmax * 4 * J));
-    HX_ST(dalloc(c, &c->part_ll, (size_t)(c->Ipad / ACC_THREADS) * c->S_q));
+    HX_ST(dalloc(c, &c->part_ll, (size_t)std::max<int64_t>((c->Ipad / ACC_THREADS) * c->S_q,
+                                                            (int64_t)loglik_f32x2_blocks(c->Ipad, K) * c->S_ll)));
     HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (2 * HX_QMAX * HX_QMAX + HX_QMAX)));
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));

@@ -13,6 +13,12 @@ int loglik_f32x2_blocks(int64_t Ipad, int K) {
     return (int)((Ipad + per - 1) / per);
 }
 
+int loglik_f32x2_resident(int K) {
+#define HX_CASE(KK) case KK: return resident_ctas((const void*)k_loglik2<KK, 2>, ACC_THREADS, 0, 0);
+    switch (K) { HX_FOR_K(HX_CASE) default: return 1; }
+#undef HX_CASE
+}
+
 cudaError_t launch_loglik_f32x2(int K, const PassArgs& a, cudaStream_t st) {
     dim3 grid((unsigned)loglik_f32x2_blocks(a.Ipad, K), (unsigned)a.S);
 #define HX_CASE(KK) case KK: k_loglik2<KK, 2><<<grid, ACC_THREADS, 0, st>>>(a); break;

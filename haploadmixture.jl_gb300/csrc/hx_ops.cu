@@ -830,6 +830,28 @@ cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st) 
     k_f2d<<<nblk(n, 256), 256, 0, st>>>(a, n, out);
     return cudaGetLastError();
 }
+int resident_ctas(const void* kernel, int threads, size_t dyn_smem, int tmem_cols) {
+    cudaFuncAttributes at{};
+    int dev = 0, regs_sm = 0, smem_sm = 0, resv = 0, thr_sm = 0, blk_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaFuncGetAttributes(&at, kernel) != cudaSuccess) return 1;
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
+    const int warps = (threads + 31) / 32;
+    int n = std::min(blk_sm, thr_sm / (32 * warps));
+    const int rwarp = ((at.numRegs + 7) / 8 * 8 * 32 + 255) / 256 * 256;   // registers of one warp
+    if (rwarp > 0) {
+        const int wsub = (regs_sm / 4) / rwarp;                               // warps per sub-partition
+        n = std::min(n, 4 * wsub / warps);
+    }
+    const size_t per = at.sharedSizeBytes + dyn_smem + (size_t)resv;
+    if (per > 0) n = std::min(n, (int)((size_t)smem_sm / per));
+    if (tmem_cols > 0) n = std::min(n, 512 / tmem_cols);
+    return std::max(n, 1);
+}
+
 cudaError_t init_kernel_attrs() {
     cudaError_t e = cudaFuncSetAttribute(k_qp_p<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(QP_WARPS * qp_warp_bytes(4 * HX_KMAX)));

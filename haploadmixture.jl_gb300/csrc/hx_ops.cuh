@@ -20,11 +20,20 @@ cudaError_t launch_accum_p_f32(int K, bool hess, const PassArgs& a, cudaStream_t
 cudaError_t launch_loglik_f32(int K, const PassArgs& a, cudaStream_t st);
 cudaError_t launch_loglik_f32x2(int K, const PassArgs& a, cudaStream_t st);   // several individuals per thread
 int loglik_f32x2_blocks(int64_t Ipad, int K);
+int loglik_f32x2_resident(int K);   // CTAs of launch_loglik_f32x2 resident on one SM
+// CTAs of a kernel resident on one SM of the current device, from its
+// registers (8-register steps per thread, 256-register steps per warp, a
+// quarter of the file per SM sub-partition), its shared memory (static +
+// dynamic + the driver's reserve), its threads and, for kernels that
+// allocate them, TMEM columns (512 per SM).  The runtime's occupancy
+// calculator reports one CTA for the tensor-core passes where the hardware
+// holds two, so the limits are applied here.
+int resident_ctas(const void* kernel, int threads, size_t dyn_smem, int tmem_cols);
 
 // tensor-core (tcgen05) Hessian+gradient passes of the mixed method (hx_tc.cu)
 // Host operations on the tensor-core instantiation of one K (hx_tc_impl.cuh);
 // each hx_tc_g*.cu unit serves a few values of K.
-enum TcOp { TC_ATTRS, TC_IMG_BYTES, TC_Q, TC_P };
+enum TcOp { TC_ATTRS, TC_IMG_BYTES, TC_Q, TC_P, TC_RESIDENT_Q, TC_RESIDENT_P };
 struct TcCall {
     TcOp op;
     int K;
@@ -40,6 +49,9 @@ cudaError_t tc_run_g3(TcCall& c);   // K = 10
 cudaError_t tc_run_g4(TcCall& c);   // K = 11
 cudaError_t tc_run_g5(TcCall& c);   // K = 12
 cudaError_t init_tc_attrs();
+// CTAs of the Hessian tensor-core pass resident on one SM (registers, shared
+// memory and TMEM columns), after init_tc_attrs
+int tc_resident(int K, bool p_side);
 
 cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st);
 

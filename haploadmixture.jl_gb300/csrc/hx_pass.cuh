@@ -340,11 +340,13 @@ k_loglik2(PassArgs a) {
     const int w0 = blockIdx.y * a.per_chunk;
     const int w1 = min(a.JW, w0 + a.per_chunk);
     uint64_t qd[NU][K];
-    float mant[NU];
+    // lmin: smallest pair likelihood (0 -> log 0 = -inf, < 0 -> NaN); chk
+    // turns NaN once any likelihood is NaN or infinite (L * 0).  Flagged
+    // products are replaced at the end, so no per-pair branch is needed.
+    float mant[NU], lmin[NU], chk[NU];
     int ex[NU];
-    bool zero[NU], bad[NU];
 #pragma unroll
-    for (int u = 0; u < NU; ++u) { mant[u] = 1.f; ex[u] = 0; zero[u] = false; bad[u] = false; }
+    for (int u = 0; u < NU; ++u) { mant[u] = 1.f; ex[u] = 0; lmin[u] = 1.f; chk[u] = 0.f; }
 #pragma unroll
     for (int u = 0; u < NU; ++u)
 #pragma unroll
@@ -389,11 +391,9 @@ k_loglik2(PassArgs a) {
                     float qp[4];
                     f2_split(z01[u], qp[0], qp[1]);
                     f2_split(z23[u], qp[2], qp[3]);
-                    float L = pair_lik_tab(nib, qp, s_snp);
-                    if (!(L > 0.f)) {
-                        if (L == 0.f) zero[u] = true; else bad[u] = true;
-                        L = 1.f;
-                    }
+                    const float L = pair_lik_tab(nib, qp, s_snp);
+                    lmin[u] = fminf(lmin[u], L);
+                    chk[u] = fmaf(L, 0.f, chk[u]);
                     mant[u] = renorm(mant[u] * L, ex[u]);
                 }
             }
@@ -404,8 +404,8 @@ k_loglik2(PassArgs a) {
     for (int u = 0; u < NU; ++u) {
         if (ii[u] < a.I) {
             double x = log((double)mant[u]) + (double)ex[u] * 0.69314718055994530942;
-            if (zero[u]) x = -INFINITY;
-            if (bad[u]) x = NAN;
+            if (lmin[u] == 0.f) x = -INFINITY;
+            if (lmin[u] < 0.f || chk[u] != chk[u]) x = NAN;
             v += x;
         }
     }

@@ -24,6 +24,11 @@ cudaError_t init_tc_attrs() {
     return cudaSuccess;
 }
 
+int tc_resident(int K, bool p_side) {
+    TcCall c{p_side ? TC_RESIDENT_P : TC_RESIDENT_Q, K, true, nullptr, nullptr, 0, 0, 0};
+    return tc_run_any(c) == cudaSuccess ? (int)c.bytes : 1;
+}
+
 size_t tc_image_bytes(int K, int64_t I, int64_t J) {
     TcCall c{TC_IMG_BYTES, K, true, nullptr, nullptr, I, J, 0};
     return tc_run_any(c) == cudaSuccess ? c.bytes : 0;

@@ -921,6 +921,12 @@ cudaError_t tc_run(TcCall& c) {
                                      (int)smem_p<K>());
         return e;
     }
+    case TC_RESIDENT_Q:
+        c.bytes = (size_t)resident_ctas((const void*)k_accum_q_tc<K, true>, TC_THREADS, smem_q<K>(), QpDims<K>::TCOLS);
+        return cudaSuccess;
+    case TC_RESIDENT_P:
+        c.bytes = (size_t)resident_ctas((const void*)k_accum_p_tc<K, true>, TC_THREADS, smem_p<K>(), TcDims<K>::TCOLS_S);
+        return cudaSuccess;
     case TC_IMG_BYTES: {
         const int64_t JW = (c.J + 7) / 8, ng = (c.I + KD - 1) / KD;
         c.bytes = std::max((size_t)JW * qimg_bytes<K>(), (size_t)ng * pimg_bytes<K>());

@@ -170,6 +170,28 @@ def test_mixed_precision_passes(hx, O, coh):
     assert rel_err(Xtz, oz) < 1e-5 and rel_err(XtX, oX) < 1e-3
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_loglik_zero_and_nan_likelihoods(hx, O, coh, precision):
+    # log of a zero pair likelihood is -inf, of a NaN one NaN, as the
+    # reference's FP64 logs (src/loops.jl:236-258)
+    b = O.Bed(coh["bed"], coh["I"], coh["J"])
+    K = coh["K"]
+    q, p = start(coh)
+    d = make(hx, coh, precision=precision)
+    p0 = p.copy()
+    p0[:, 0] = 0.0                       # qp00 = 0 in block 0 for everyone
+    assert np.isneginf(O.loglik(b, K, q, p0))
+    assert np.isneginf(d.loglikelihood(q, p0))
+    q1 = q.copy()
+    q1[0, 5] = np.nan
+    assert np.isnan(O.loglik(b, K, q1, p))
+    assert np.isnan(d.loglikelihood(q1, p))
+    p1 = p0.copy()
+    p1[:, 4 * coh["J"] - 1] = np.nan     # NaN and zero likelihoods together: NaN
+    assert np.isnan(d.loglikelihood(q, p1))
+    assert d.loglikelihood(q, p) == pytest.approx(O.loglik(b, K, q, p), rel=1e-8 if precision == "mixed" else 1e-12)
+
+
 def test_mixed_fit_reaches_fp64_optimum(hx, O):
     # both fits run to (near) full convergence, so that the comparison is
     # between optima and not between two early-stopped points of a flat
