@@ -738,7 +738,10 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
     constexpr int QSTR = qstr<K>();
     constexpr int GB = pimg_bytes<K>();
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    // aligned by an offset from the shared array (no integer round trip), so
+    // that the compiler keeps every derived pointer in the shared space:
+    // 32-bit shared loads instead of generic ones (fewer registers, no spills)
+    uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     const uint32_t sA = smem_u32(smem);                              // [2][4][A_TILE_PAD]
     const uint32_t sR = sA + 2 * 4 * A_TILE_PAD;                     // ring [RING][GB]
     uint32_t* SW = (uint32_t*)(smem + (sR - sA) + RING * GB);        // [RING][4][KD]
