@@ -31,8 +31,8 @@
 //
 // Pipeline per stage, with no CTA-wide barrier in the loop: every thread waits
 // for the stage's ring slot and until the MMAs that last read its A buffer
-// (stage s-2) are done; thread 0 then refills the ring slot of stage s-2 with
-// stage s-2+RING; every warp generates its part of the A tiles and arrives on
+// (stage s-2) are done; the first warp to get there refills the ring slot of
+// stage s-2 with stage s-2+RING; every warp generates its part of the A tiles and arrives on
 // a shared counter; the last arriving warp issues the stage's MMAs and commits
 // them to an mbarrier.  Warps therefore run up to two stages apart, and two CTAs (16 warps)
 // share an SM.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
@@ -114,6 +114,7 @@ struct Sync {
     int loaded;            // stages whose input copies have been issued
     int loadedq;           // Q side: stages whose qp p tile copy has been issued
     uint32_t arrived[2];   // generator arrivals on stage buffer b (monotonic)
+    uint32_t started[2];   // warps past the waits of a stage, by stage parity (the first one refills)
     // stage-input sources, read only by the thread that issues a refill
     const uint8_t* img0;   // image slice of stage 0
     const uint32_t* g0;    // class words of stage 0
@@ -139,6 +140,20 @@ __device__ __forceinline__ bool arrive_last(uint32_t* ctr) {
         last = (old % (TC_THREADS / 32)) == TC_THREADS / 32 - 1;
     }
     return last;
+}
+
+// True in lane 0 of the first warp of the CTA to reach this point of a stage
+// (one atomic per warp).  Counted by stage parity like arrive_last: a warp
+// reaches stage s+2 only after every warp has passed this point of stage s.
+__device__ __forceinline__ bool first_at_stage(uint32_t* ctr) {
+    __syncwarp();
+    bool first = false;
+    if ((threadIdx.x & 31) == 0) {
+        uint32_t old;
+        asm volatile("atom.relaxed.cta.shared::cta.add.u32 %0, [%1], 1;" : "=r"(old) : "r"(smem_u32(ctr)) : "memory");
+        first = (old % (TC_THREADS / 32)) == 0;
+    }
+    return first;
 }
 
 __device__ __forceinline__ void set_bad(Sync* sy, double* slots) {
@@ -439,6 +454,8 @@ __device__ __forceinline__ void init_sync(Sync* sy, int tid) {
         sy->loaded = 0;
         sy->arrived[0] = 0;
         sy->arrived[1] = 0;
+        sy->started[0] = 0;
+        sy->started[1] = 0;
         mbar_fence_init();
     }
 }
@@ -558,7 +575,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         expect_tx(&sy->full[slot], (uint32_t)(GBM + 512));
         bulk_copy(sR + slot * GBM, sy->img0 + (int64_t)t * GB, GBM, &sy->full[slot]);
         bulk_copy(smem_u32(SW + slot * 128), sy->g0 + (int64_t)t * sy->gstride, 512, &sy->full[slot]);
-        sy->loaded = t + 1;
+        atomicMax(&sy->loaded, t + 1);   // refills come from different warps
     };
     auto load_qtile = [&](int t) {
         const int slot = t % QRING;
@@ -626,8 +643,10 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         if (is_bad(sy)) break;
         // ring refill: the slot of stage s-2 is free (its MMAs are done -- just
-        // waited for -- and they were issued after every thread had read it)
-        if (tid == 0 && s >= 2 && s - 2 + RING < ns) load_stage(s - 2 + RING);
+        // waited for -- and they were issued after every thread had read it).
+        // The first warp here loads it, which keeps the refill off the last
+        // arriving warp of stage s-1 (the MMA issuer, still issuing).
+        if (s >= 2 && s - 2 + RING < ns && first_at_stage(&sy->started[b])) load_stage(s - 2 + RING);
         const uint32_t word = SW[slot * 128 + r];
         // this stage's qp: 16 columns of this thread's row
         float qpv[16];
@@ -771,7 +790,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         for (int w = 0; w < sy->nwc; ++w)
             bulk_copy(smem_u32(SW + (slot * 4 + w) * KD), sy->g0 + w * sy->gstride + (int64_t)KD * t, 128,
                       &sy->full[slot]);
-        sy->loaded = t + 1;
+        atomicMax(&sy->loaded, t + 1);   // refills come from different warps
     };
 
     if (warp == 0) tmem_alloc<D::TCOLS_S>(&sy->tslot);
@@ -811,8 +830,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
         if (s >= 2 && !is_bad(sy))
             if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
         if (is_bad(sy)) break;
-        // ring refill (see the Q side)
-        if (tid == 0 && s >= 2 && s - 2 + RING < ns) load_stage(s - 2 + RING);
+        // ring refill by the first warp here (see the Q side)
+        if (s >= 2 && s - 2 + RING < ns && first_at_stage(&sy->started[b])) load_stage(s - 2 + RING);
         const float* Qs = reinterpret_cast<const float*>(smem + (sR - sA) + slot * GB + 2 * D::B_TILE);
         const uint32_t* Ws = SW + slot * 4 * KD + (jl >> 3) * KD;
         // A = W^T tile: rows m = 4*jl + h, reduction over the stage's individuals
