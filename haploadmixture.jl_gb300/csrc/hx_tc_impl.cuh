@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         const int slot = t % QRING;
         expect_tx(&sy->fullq[slot], (uint32_t)GBQ);
         bulk_copy(sRq + slot * GBQ, sy->img0 + (int64_t)t * GB + GBM, GBQ, &sy->fullq[slot]);
-        sy->loadedq = t + 1;
+        atomicMax(&sy->loadedq, t + 1);
     };
 
     if (warp == 0) tmem_alloc<QD::TCOLS>(&sy->tslot);
@@ -646,13 +646,22 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         // waited for -- and they were issued after every thread had read it).
         // The first warp here loads it, which keeps the refill off the last
         // arriving warp of stage s-1 (the MMA issuer, still issuing).
-        if (s >= 2 && s - 2 + RING < ns && first_at_stage(&sy->started[b])) load_stage(s - 2 + RING);
+        // The qp tile slot of stage s is free too: its MMA (issued with the
+        // MMAs of stage s-2) is done.
+        if (s >= 2 && first_at_stage(&sy->started[b])) {
+            if (s - 2 + RING < ns) load_stage(s - 2 + RING);
+            if (s + QRING < ns) load_qtile(s + QRING);
+        }
         const uint32_t word = SW[slot * 128 + r];
-        // this stage's qp: 16 columns of this thread's row
+        // this stage's qp: 16 columns of this thread's row.  From stage 2 on it
+        // was issued with the MMAs of stage s-2 and is covered by their
+        // mma_done, just waited for; stages 0 and 1 wait for the prologue's.
         float qpv[16];
         {
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], (s >> 1) & 1, TC_BUDGET));
-            if (!ok) { set_bad(sy, a.slots); break; }
+            if (s < 2) {
+                const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], 0, TC_BUDGET));
+                if (!ok) { set_bad(sy, a.slots); break; }
+            }
             fence_after();
             tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16), qpv);
             tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16 + 8), qpv + 8);
@@ -689,17 +698,16 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             if (s + 2 < ns) {
                 const int qs = (s + 2) % QRING;
                 if (!mbar_wait(&sy->fullq[qs], ((s + 2) / QRING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
-                else {
-                    issue_qp<K>(tq + b * 32, sAq, sRq + qs * GBQ);
-                    commit(&sy->qp_done[b]);
-                }
+                else issue_qp<K>(tq + b * 32, sAq, sRq + qs * GBQ);
             }
             const int d = (s / TC_FLUSH) & 1;
             issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, (s % TC_FLUSH) == 0);
             // mma_done also covers the qp MMA, so that draining it covers every MMA in flight
             commit_stage(sy, s, ns, b);
-            // the qp tile slot of stage s is free (its MMA is done: every thread waited for it)
-            if (s + QRING < ns) load_qtile(s + QRING);
+            // the qp tile slots of stages 0 and 1 (their MMAs came from the
+            // prologue, every thread waited for them); later ones are refilled
+            // by the first warp of the stage
+            if (s < 2 && s + QRING < ns) load_qtile(s + QRING);
         }
         maybe_fold<K, false>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
