@@ -70,6 +70,9 @@ __device__ __forceinline__ void bulk_load(uint32_t dst_smem, const void* src, ui
 __device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(m)), "r"(count));
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* m) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(m)) : "memory");
+}
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // Bounded wait for the phase with the given parity; false on timeout.

@@ -108,6 +108,7 @@ struct Sync {
     uint64_t mma_done[2];
     uint64_t flush_done[2];
     uint64_t qp_done[2];
+    uint64_t gen_full[2];  // the 8 generator warps have written stage buffer b (one arrival per warp)
     uint32_t tslot;
     int bad;
     int issued;            // stages whose MMAs have been issued
@@ -244,38 +245,38 @@ __device__ __forceinline__ void compensate(float* acc, const float* comp) {
     }
 }
 
-// Issues the 3 split products of one 32-deep stage into D (TMEM cols dcol..):
+// The 3 split products of one 32-deep stage into D (TMEM cols dcol..):
 // Hessian (N = NHP, bf16) and gradient (N = 16, fp16).  A tiles W_hi, W_lo,
 // U_hi, U_lo at aBase + t*aStride; B tiles: hi at bBase, lo at bBase + B_TILE.
-template <int K, bool HESS>
-__device__ __forceinline__ void issue_stage(uint32_t tmem, int dcol, uint32_t aBase, int aStride, int aLBO, int aSBO,
-                                            uint32_t bBase, bool first) {
+// Issued in two groups with disjoint accumulator columns, by two issuers: the
+// Hessian's (HG = 0) and the gradient's (HG = 1).  Each column keeps one
+// issuer, issuing in stage order, so the FP32 accumulation order is fixed
+// (bit-reproducible).
+template <int K, int HG>
+__device__ __forceinline__ void issue_stage_group(uint32_t tmem, int dcol, uint32_t aBase, int aStride, int aLBO,
+                                                  int aSBO, uint32_t bBase, bool first) {
     using D = TcDims<K>;
     constexpr uint32_t idH = idesc_bf16(D::NHP);
     constexpr uint32_t idG = idesc_f16(D::NG);
     const uint32_t dH = tmem + dcol;
     const uint32_t dG = tmem + dcol + D::NHP;
-    const uint32_t bPPh = bBase, bPPl = bBase + D::B_TILE;
-    const uint32_t bPh = bBase + (D::NHP / 8) * SBO_STD, bPl = bPh + D::B_TILE;
-    // descriptors of other addresses: the 14-bit address field (bytes >> 4)
-    // of one base descriptor plus the offset >> 4 (shared memory < 256 KB)
     const uint64_t dA = sdesc(aBase, aLBO, aSBO), dB = sdesc(bBase, LBO_STD, SBO_STD);
     const uint64_t oS = (uint64_t)(aStride >> 4), oBl = (uint64_t)(D::B_TILE >> 4);
-    const uint64_t oPh = (uint64_t)((bPh - bBase) >> 4);
-    (void)bPPh; (void)bPPl; (void)bPl;
+    const uint64_t oPh = (uint64_t)(((D::NHP / 8) * SBO_STD) >> 4);
 #pragma unroll
     for (int ks = 0; ks < KD / 16; ++ks) {
         const uint64_t ao = (uint64_t)((ks * 2 * aLBO) >> 4), bo = (uint64_t)((ks * 2 * LBO_STD) >> 4);
         const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
         const uint64_t aWh = dA + ao, aWl = aWh + oS, aUh = aWh + 2 * oS, aUl = aWh + 3 * oS;
-        if (HESS) {
+        if (HG == 0) {
             mma_bf16(dH, aWh, dB + bo, idH, acc0);
             mma_bf16(dH, aWh, dB + oBl + bo, idH, 1u);
             mma_bf16(dH, aWl, dB + bo, idH, 1u);
+        } else {
+            mma_bf16(dG, aUh, dB + oPh + bo, idG, acc0);
+            mma_bf16(dG, aUh, dB + oPh + oBl + bo, idG, 1u);
+            mma_bf16(dG, aUl, dB + oPh + bo, idG, 1u);
         }
-        mma_bf16(dG, aUh, dB + oPh + bo, idG, acc0);
-        mma_bf16(dG, aUh, dB + oPh + oBl + bo, idG, 1u);
-        mma_bf16(dG, aUl, dB + oPh + bo, idG, 1u);
     }
 }
 
@@ -441,13 +442,16 @@ __global__ void __launch_bounds__(128) k_pimg(const double* __restrict__ q, int6
 }
 
 // ------------------------------------------------------------------ shared helpers
-__device__ __forceinline__ void init_sync(Sync* sy, int tid) {
+// n_mma: issuers that commit each stage to mma_done; n_flush: those that
+// commit each accumulator window to flush_done
+__device__ __forceinline__ void init_sync(Sync* sy, int tid, int n_mma, int n_flush) {
     if (tid == 0) {
         for (int r = 0; r < RING; ++r) mbar_init(&sy->full[r], 1);
         for (int r = 0; r < QRING; ++r) mbar_init(&sy->fullq[r], 1);
         sy->loadedq = 0;
-        mbar_init(&sy->mma_done[0], 1); mbar_init(&sy->mma_done[1], 1);
-        mbar_init(&sy->flush_done[0], 1); mbar_init(&sy->flush_done[1], 1);
+        mbar_init(&sy->mma_done[0], n_mma); mbar_init(&sy->mma_done[1], n_mma);
+        mbar_init(&sy->flush_done[0], n_flush); mbar_init(&sy->flush_done[1], n_flush);
+        mbar_init(&sy->gen_full[0], TC_THREADS / 32); mbar_init(&sy->gen_full[1], TC_THREADS / 32);
         mbar_init(&sy->qp_done[0], 1); mbar_init(&sy->qp_done[1], 1);
         sy->bad = 0;
         sy->issued = 0;
@@ -469,11 +473,26 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 }
 
 // Window bookkeeping after a stage's MMAs were issued by this thread.
-__device__ __forceinline__ void commit_stage(Sync* sy, int s, int ns, int b) {
+__device__ __forceinline__ void commit_stage(Sync* sy, int s, int ns, int b, bool window = true) {
     const int d = (s / TC_FLUSH) & 1;
     commit(&sy->mma_done[b]);
-    if ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1) commit(&sy->flush_done[d]);
-    sy->issued = s + 1;
+    if (window && ((s % TC_FLUSH) == TC_FLUSH - 1 || s == ns - 1)) commit(&sy->flush_done[d]);
+    atomicMax(&sy->issued, s + 1);
+}
+
+// Every generator warp has written its part of stage s's A tiles (buffer b):
+// one arrival per warp, after the tiles are made visible to the tensor core.
+__device__ __forceinline__ void arrive_generated(Sync* sy, int b) {
+    fence_async_smem();
+    fence_before();
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&sy->gen_full[b]);
+}
+// An issuer (lane 0 of a fixed warp) waits until the whole stage is generated.
+__device__ __forceinline__ bool wait_generated(Sync* sy, int s, int b, double* slots) {
+    if (!mbar_wait(&sy->gen_full[b], (s >> 1) & 1, TC_BUDGET)) { set_bad(sy, slots); return false; }
+    fence_after();
+    return true;
 }
 
 // Fold of TMEM window w at stage (w+1)*TC_FLUSH + FOLD_OFF: half a window
@@ -585,7 +604,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     };
 
     if (warp == 0) tmem_alloc<QD::TCOLS>(&sy->tslot);
-    init_sync(sy, tid);
+    init_sync(sy, tid, HESS ? 3 : 2, HESS ? 2 : 1);   // issuers: Hessian, gradient, qp
     if (tid == 0) {
         sy->img0 = a.img + (int64_t)w0 * GB;
         sy->g0 = a.G + (int64_t)w0 * a.Ipad + i0;
@@ -689,25 +708,34 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             sts128(aB + 2 * A_TILE_STD + off, uh[0], uh[1], uh[2], uh[3]);
             sts128(aB + 3 * A_TILE_STD + off, ul[0], ul[1], ul[2], ul[3]);
         }
-        fence_async_smem();
-        fence_before();
-        if (arrive_last(&sy->arrived[b])) {
-            fence_after();
-            // qp of stage s+2 into this stage's qp columns (every thread has read
-            // them), ahead of this stage's MMAs
-            if (s + 2 < ns) {
-                const int qs = (s + 2) % QRING;
-                if (!mbar_wait(&sy->fullq[qs], ((s + 2) / QRING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
-                else issue_qp<K>(tq + b * 32, sAq, sRq + qs * GBQ);
+        arrive_generated(sy, b);
+        // Three issuers, lane 0 of warps 0, 2 and 4, each with its own TMEM
+        // columns: the Hessian MMAs, the gradient MMAs, and the qp MMA of stage
+        // s+2 into this stage's qp columns (every thread has read them).  Each
+        // commits to mma_done, which therefore also covers the qp MMA.
+        if ((tid & 31) == 0 && (warp == 2 || warp == 4 || (HESS && warp == 0))) {
+            if (wait_generated(sy, s, b, a.slots)) {
+                const int d = (s / TC_FLUSH) & 1;
+                if (warp == 4) {
+                    if (s + 2 < ns) {
+                        const int qs = (s + 2) % QRING;
+                        if (!mbar_wait(&sy->fullq[qs], ((s + 2) / QRING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+                        else issue_qp<K>(tq + b * 32, sAq, sRq + qs * GBQ);
+                    }
+                    commit_stage(sy, s, ns, b, false);
+                    // the qp tile slots of stages 0 and 1 (their MMAs came from the
+                    // prologue, every thread waited for them); later ones are
+                    // refilled by the first warp of the stage
+                    if (s < 2 && s + QRING < ns) load_qtile(s + QRING);
+                } else {
+                    const bool first = (s % TC_FLUSH) == 0;
+                    if (warp == 0)
+                        issue_stage_group<K, 0>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, first);
+                    else
+                        issue_stage_group<K, 1>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, first);
+                    commit_stage(sy, s, ns, b);
+                }
             }
-            const int d = (s / TC_FLUSH) & 1;
-            issue_stage<K, HESS>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, (s % TC_FLUSH) == 0);
-            // mma_done also covers the qp MMA, so that draining it covers every MMA in flight
-            commit_stage(sy, s, ns, b);
-            // the qp tile slots of stages 0 and 1 (their MMAs came from the
-            // prologue, every thread waited for them); later ones are refilled
-            // by the first warp of the stage
-            if (s < 2 && s + QRING < ns) load_qtile(s + QRING);
         }
         maybe_fold<K, false>(sy, a.slots, hf, s, taddr_lane, acc, comp);
     }
@@ -802,7 +830,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
     };
 
     if (warp == 0) tmem_alloc<D::TCOLS_S>(&sy->tslot);
-    init_sync(sy, tid);
+    init_sync(sy, tid, 1, 1);
     if (tid == 0) {
         sy->img0 = a.img + g0 * GB;
         sy->g0 = a.G + jw0 * a.Ipad + i0;
@@ -879,6 +907,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
             asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + 2 * A_TILE_PAD + off), "r"(uh[0]), "r"(uh[1]) : "memory");
             asm volatile("st.shared.v2.b32 [%0], {%1, %2};" :: "r"(aB + 3 * A_TILE_PAD + off), "r"(ul[0]), "r"(ul[1]) : "memory");
         }
+        // One issuer, the last warp to arrive: on this side two issuers were
+        // measured slower (the SM's MMA issue rate, not one thread, is the
+        // limit, and the fixed issuer warps fall behind on generation)
         fence_async_smem();
         fence_before();
         if (arrive_last(&sy->arrived[b])) {
