@@ -149,7 +149,7 @@ def pass_flops(I, J, K):
 # Hessian passes, from one-pass ncu captures of one launch each at I=100,000,
 # J=100,000, K=8 (profiles/k_accum_tc_c3_dram.md): P 5.65 GB, Q 5.83 GB per
 # launch over 1e10 pairs.
-TRAFFIC_PER_PAIR = {"accum_q": 0.583, "accum_p": 0.565}
+TRAFFIC_PER_PAIR = {"accum_q": 0.592, "accum_p": 0.588}
 
 
 def workload(name, cfg):
