@@ -35,6 +35,7 @@ struct hx_ctx {
     double *U = nullptr, *V = nullptr;
     double *XtXq = nullptr, *Xtzq = nullptr, *XtXp = nullptr, *Xtzp = nullptr;
     double *part_q = nullptr, *part_p = nullptr, *part_ll = nullptr, *part_qn = nullptr, *coef = nullptr;
+    float* pf = nullptr;                     // mixed: FP32 copy of the pass's p (K x 4J)
     double* slots = nullptr;
     double* h_slots = nullptr;   // pinned
     uint8_t* img = nullptr;      // B-operand image of the tensor-core passes
@@ -180,7 +181,15 @@ PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
     a.part = nullptr; a.XtX = nullptr; a.Xtz = nullptr;
     a.slots = c->slots;
     a.img = c->img;
+    a.pf = nullptr;
     return a;
+}
+
+// The FP32 passes that stage p per CTA read this FP32 copy of it.
+int stage_pf(hx_ctx* c, const double* p, PassArgs& a) {
+    HX_LAUNCH(HX_KIND_OTHER, 1, launch_d2f(p, (int64_t)c->K * 4 * c->J, c->pf, c->st));
+    a.pf = c->pf;
+    return HX_OK;
 }
 
 int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, double* Xtz) {
@@ -193,6 +202,7 @@ int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
         return HX_OK;
     }
     a.S = c->S_q; a.per_chunk = c->wpc_q; a.part = c->part_q;
+    if (c->prec != HX_PREC_FP64) HX_ST(stage_pf(c, p, a));
     HX_LAUNCH(HX_KIND_ACCUM_Q, 1,
               c->prec == HX_PREC_FP64 ? launch_accum_q_f64(c->K, hess, a, c->st)
                                       : launch_accum_q_f32(c->K, hess, a, c->st));
@@ -229,6 +239,7 @@ int loglik_to_slot(hx_ctx* c, const double* q, const double* p, int slot) {
                   launch_reduce_sum(c->part_ll, (c->Ipad / ACC_THREADS) * c->S_q, c->slots + slot, c->st));
     } else {
         a.S = c->S_ll; a.per_chunk = c->wpc_ll;
+        HX_ST(stage_pf(c, p, a));
         HX_LAUNCH(HX_KIND_LOGLIK, 1, launch_loglik_f32x2(c->K, a, c->st));
         HX_LAUNCH(HX_KIND_OTHER, 1,
                   launch_reduce_sum(c->part_ll, (int64_t)loglik_f32x2_blocks(c->Ipad, c->K) * c->S_ll, c->slots + slot,
@@ -434,6 +445,7 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));
     if (c->tc) HX_ST(dalloc(c, &c->img, tc_image_bytes(K, I, J)));
+    if (c->prec != HX_PREC_FP64) HX_ST(dalloc(c, &c->pf, (size_t)K * 4 * J));
     HX_ST(dalloc(c, &c->qp_ws, (size_t)4 * K * J));
     HX_CK(cudaMemsetAsync(c->qp_ws, 0, (size_t)4 * K * J, c->st));
     HX_CK(cudaMallocHost((void**)&c->h_slots, HX_NSLOT * sizeof(double)));
@@ -559,7 +571,8 @@ int hx_destroy(hx_ctx* c) {
     if (!c) return HX_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     void* bufs[] = {c->shared_geno ? nullptr : (void*)c->G, c->shared_geno ? nullptr : (void*)c->dm, c->x, c->xn, c->xn2, c->xt, c->xio, c->U, c->V, c->XtXq, c->Xtzq, c->XtXp,
-                    c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots, c->img, c->qp_ws};
+                    c->Xtzp, c->part_q, c->part_p, c->part_ll, c->part_qn, c->coef, c->slots, c->img, c->qp_ws,
+                    c->pf};
     for (void* b : bufs) if (b) cudaFree(b);
     prof_resolve(c);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);

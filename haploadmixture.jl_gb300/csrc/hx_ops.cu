@@ -830,6 +830,14 @@ cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st) 
     k_f2d<<<nblk(n, 256), 256, 0, st>>>(a, n, out);
     return cudaGetLastError();
 }
+__global__ void k_d2f(const double* __restrict__ a, int64_t n, float* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = (float)a[t];
+}
+cudaError_t launch_d2f(const double* a, int64_t n, float* out, cudaStream_t st) {
+    k_d2f<<<nblk(n, 256), 256, 0, st>>>(a, n, out);
+    return cudaGetLastError();
+}
 int resident_ctas(const void* kernel, int threads, size_t dyn_smem, int tmem_cols) {
     cudaFuncAttributes at{};
     int dev = 0, regs_sm = 0, smem_sm = 0, resv = 0, thr_sm = 0, blk_sm = 0;

@@ -54,6 +54,7 @@ cudaError_t init_tc_attrs();
 int tc_resident(int K, bool p_side);
 
 cudaError_t launch_f2d(const float* a, int64_t n, double* out, cudaStream_t st);
+cudaError_t launch_d2f(const double* a, int64_t n, float* out, cudaStream_t st);
 
 // learned warm start (hx_lws.cu)
 cudaError_t lws_attrs();

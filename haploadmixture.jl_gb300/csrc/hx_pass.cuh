@@ -47,6 +47,8 @@ struct PassArgs {
     double* Xtz;
     double* slots;          // per-context scalar block (tensor-core kernels record timeouts there)
     uint8_t* img;           // tensor-core passes: B-operand image of the pass (written by the pass)
+    const float* pf;        // FP32 copy of p for the FP32 passes that stage p (or null): GB300's
+                            // FP64 unit is narrow, and converting in every CTA kept it busy
 };
 
 template <int K> __device__ __forceinline__ constexpr int tri(int k, int k2) {
@@ -89,7 +91,7 @@ k_accum_q(PassArgs a) {
         const int64_t base = (int64_t)ws * 8 * 4 * K;
         const int64_t limit = a.J * 4 * K;
         for (int t = tid; t < nval; t += ACC_THREADS)
-            sp[t] = (base + t < limit) ? (T)a.p[base + t] : T(0.25);
+            sp[t] = (base + t < limit) ? ((sizeof(T) == 4 && a.pf) ? (T)a.pf[base + t] : (T)a.p[base + t]) : T(0.25);
         __syncthreads();
         if (active) {
             for (int w = 0; w < nw; ++w) {
@@ -275,7 +277,7 @@ k_loglik(PassArgs a) {
         const int64_t base = (int64_t)ws * 8 * 4 * K;
         const int64_t limit = a.J * 4 * K;
         for (int t = tid; t < nval; t += ACC_THREADS)
-            sp[t] = (base + t < limit) ? (T)a.p[base + t] : T(0.25);
+            sp[t] = (base + t < limit) ? ((sizeof(T) == 4 && a.pf) ? (T)a.pf[base + t] : (T)a.p[base + t]) : T(0.25);
         __syncthreads();
         if (active) {
             for (int w = 0; w < nw; ++w) {
@@ -366,7 +368,7 @@ k_loglik2(PassArgs a) {
         const int64_t limit = a.J * 4 * K;
         for (int t = tid; t < nval; t += ACC_THREADS) {
             const int blk = t / (4 * K), r = t - blk * 4 * K, h = r / K, k = r - h * K;
-            spt[blk * 4 * K + k * 4 + h] = (base + t < limit) ? (float)a.p[base + t] : 0.25f;
+            spt[blk * 4 * K + k * 4 + h] = (base + t < limit) ? (a.pf ? a.pf[base + t] : (float)a.p[base + t]) : 0.25f;
         }
         __syncthreads();
         for (int w = 0; w < nw; ++w) {
