@@ -240,7 +240,7 @@ def test_loop_options_match_oracle_fp64(hx, O, opts):
         np.testing.assert_allclose(pd, p0, rtol=0, atol=1e-15)
 
 
-@pytest.mark.parametrize("K", [2, 3, 5, 8, 12])
+@pytest.mark.parametrize("K", [1, 2, 3, 5, 8, 12])
 def test_qp_p_equality_form_matches_oracle(hx, O, K):
     # penalty = false: per block, 4K variables with the K equalities
     # sum_h d[k, h] = 0 (src/algorithms_inner.jl:307-310)
