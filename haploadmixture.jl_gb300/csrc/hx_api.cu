@@ -818,13 +818,15 @@ int hx_em_step(hx_ctx* c) {
     return HX_OK;
 }
 
-// init_em! (src/algorithms_outer.jl:1-22).
+// init_em! (src/algorithms_outer.jl:1-22).  The log-likelihood of every EM
+// iteration is only reported there; the last one seeds the QN loop.  So it is
+// evaluated after the last iteration, and after every one only when verbose.
 int hx_init_em(hx_ctx* c, int32_t iters) {
     HX_ST(check_qp(c));
     for (int e = 0; e < iters; ++e) {
         HX_ST(em_step(c));
         HX_CK(cudaMemcpyAsync(c->x, c->xn, (size_t)c->nx * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
-        HX_ST(loglik_to_slot(c, qof(c->x), pof(c, c->x), S_LL_NEW));
+        if (c->verbose || e + 1 == iters) HX_ST(loglik_to_slot(c, qof(c->x), pof(c, c->x), S_LL_NEW));
         HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_p(pof(c, c->x), nullptr, c->K, c->J, c->eps, pof(c, c->x), c->st));
         HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_q(qof(c->x), nullptr, c->K, c->I, c->eps, qof(c->x), c->st));
         if (c->verbose) {
