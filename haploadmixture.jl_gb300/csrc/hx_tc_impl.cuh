@@ -547,7 +547,7 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int 
 // qp[i, m] = sum_k q[k,i] p[k,m] also comes from the tensor core: kind::tf32
 // MMAs (hi*hi + hi*lo + lo*hi of TF32-rounded splits, ~2^-21 relative) of the
 // CTA's q tile by the stage's p tile into a double-buffered 32-column TMEM
-// tile, issued one stage ahead; each thread reads its row's 16 values.
+// tile, issued two stages ahead; each thread reads its row's 16 values.
 
 // One pair from its qp: U (scaled) and W.
 template <bool HESS>
