@@ -72,6 +72,11 @@ template <int K> struct TcDims {
     static constexpr int NT = NHP + NG;
     static constexpr int TCOLS = (2 * NT <= 32) ? 32 : (2 * NT <= 64) ? 64 : (2 * NT <= 128) ? 128 : 256;
     static constexpr int HALF = NT / 2;
+    // Q side: one TMEM window = [Hessian NHP | gradient hi.hi NG | gradient
+    // hi.lo + lo.hi NG].  Every MMA write rounds the accumulator it adds to,
+    // not to nearest, so the small lo products get columns of their own:
+    // the large hi.hi sums are written a third as often.
+    static constexpr int WQ = NT + NG;
     static constexpr int B_TILE = (NT / 8) * SBO_STD;    // NT rows x 32 x 2 B
     // P side, stacked operands: one TMEM window holds hi.hi (+ lo.hi) and hi.lo
     // of the Hessian side by side, then the same for the gradient
@@ -87,8 +92,9 @@ template <int K> struct QpDims {
     static constexpr int SBO = (KP / 4) * 128;        // 4 tf32 per 16-byte core row
     static constexpr int A_T = 16 * SBO;              // 128 rows
     static constexpr int B_T = 4 * SBO;               // 32 rows
-    static constexpr int NCOL = 2 * TcDims<K>::NT + 64;
-    static constexpr int TCOLS = NCOL <= 32 ? 32 : NCOL <= 64 ? 64 : NCOL <= 128 ? 128 : 256;
+    static constexpr int NCOL = 2 * TcDims<K>::WQ + 64;
+    static constexpr int TCOLS = NCOL <= 32 ? 32 : NCOL <= 64 ? 64 : NCOL <= 128 ? 128 : NCOL <= 256 ? 256 : 512;
+    static_assert(NCOL <= TCOLS && TCOLS <= 512, "Q-side TMEM columns");
 };
 
 // P side: staged q rows hold each q[k] twice, (q_k, q_k), as the first operand
@@ -190,6 +196,19 @@ __device__ __forceinline__ void fold(uint32_t taddr_lane, int dcol, float* acc, 
         for (int c = 0; c < D::HALF / 8; ++c)
             tmem_ld8_async(taddr_lane + (uint32_t)(dcol + HF * D::HALF + 8 * c), raw + 8 * c);
         tmem_wait_ld();
+        // gradient columns: add their lo-product columns [NT, NT + NG)
+#pragma unroll
+        for (int c = 0; c < D::HALF / 8; ++c) {
+            const int col = HF * D::HALF + 8 * c;     // chunks never straddle NHP (a multiple of 16)
+            if (col >= D::NHP) {
+                uint32_t r2[8];
+                tmem_ld8_async(taddr_lane + (uint32_t)(dcol + D::NT + (col - D::NHP)), r2);
+                tmem_wait_ld();
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    raw[8 * c + t] = __float_as_uint(__uint_as_float(raw[8 * c + t]) + __uint_as_float(r2[t]));
+            }
+        }
     } else {
 #pragma unroll
         for (int c = 0; c < D::HALF / 8; ++c) {
@@ -274,8 +293,8 @@ __device__ __forceinline__ void issue_stage_group(uint32_t tmem, int dcol, uint3
             mma_bf16(dH, aWl, dB + bo, idH, 1u);
         } else {
             mma_bf16(dG, aUh, dB + oPh + bo, idG, acc0);
-            mma_bf16(dG, aUh, dB + oPh + oBl + bo, idG, 1u);
-            mma_bf16(dG, aUl, dB + oPh + bo, idG, 1u);
+            mma_bf16(dG + D::NG, aUh, dB + oPh + oBl + bo, idG, acc0);   // lo products: own columns
+            mma_bf16(dG + D::NG, aUl, dB + oPh + bo, idG, 1u);
         }
     }
 }
@@ -300,12 +319,15 @@ __device__ __forceinline__ void issue_stage_stacked(uint32_t tmem, int dcol, uin
         const uint64_t ao = (uint64_t)((ks * 2 * aLBO) >> 4), bo = (uint64_t)((ks * 2 * LBO_STD) >> 4);
         const uint32_t acc0 = (first && ks == 0) ? 0u : 1u;
         const uint64_t aWh = dA + ao, aWl = aWh + oS, aUh = aWh + 2 * oS, aUl = aWh + 3 * oS;
+        // lo.hi adds into the hi.lo columns, so that the large hi.hi sums are
+        // written once per k-step (every MMA write rounds its accumulator,
+        // not to nearest)
         if (HESS) {
             mma_bf16(dH, aWh, dB + bo, idH2, acc0);
-            mma_bf16(dH, aWl, dB + bo, idH, 1u);
+            mma_bf16(dH + D::NHP, aWl, dB + bo, idH, 1u);
         }
         mma_bf16(dG, aUh, dB + oG + bo, idG2, acc0);
-        mma_bf16(dG, aUl, dB + oG + bo, idG, 1u);
+        mma_bf16(dG + D::NG, aUl, dB + oG + bo, idG, 1u);
     }
 }
 
@@ -504,7 +526,7 @@ template <int K, bool STACK>
 __device__ __forceinline__ void maybe_fold(Sync* sy, double* slots, int hf, int s, uint32_t taddr_lane, float* acc,
                                            float* comp) {
     using D = TcDims<K>;
-    constexpr int WC = STACK ? D::WS : D::NT;   // TMEM columns per window
+    constexpr int WC = STACK ? D::WS : D::WQ;   // TMEM columns per window
     if (s >= TC_FLUSH + FOLD_OFF && (s - FOLD_OFF) % TC_FLUSH == 0) {
         const int wp = (s - FOLD_OFF) / TC_FLUSH - 1;
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
@@ -521,7 +543,7 @@ template <int K, bool STACK>
 __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int ns, uint32_t taddr_lane, float* acc,
                                            float* comp) {
     using D = TcDims<K>;
-    constexpr int WC = STACK ? D::WS : D::NT;
+    constexpr int WC = STACK ? D::WS : D::WQ;
     __syncthreads();
     if (ns > 0 && !is_bad(sy)) {
         // windows not folded in the loop: the last one and possibly the one before
@@ -617,7 +639,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     __syncthreads();
     fence_after();
     const uint32_t tmem = sy->tslot;
-    const uint32_t tq = tmem + 2 * D::NT;                 // qp tiles: columns [2NT, 2NT + 64)
+    const uint32_t tq = tmem + 2 * D::WQ;                 // qp tiles: columns [2WQ, 2WQ + 64)
     const uint32_t taddr_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     if (tid == 0) {
         for (int t = 0; t < RING && t < ns; ++t) load_stage(t);
@@ -682,8 +704,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
                 if (!ok) { set_bad(sy, a.slots); break; }
             }
             fence_after();
-            tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16), qpv);
-            tmem_ld8(taddr_lane + (uint32_t)(2 * D::NT + b * 32 + hf * 16 + 8), qpv + 8);
+            tmem_ld8(taddr_lane + (uint32_t)(2 * D::WQ + b * 32 + hf * 16), qpv);
+            tmem_ld8(taddr_lane + (uint32_t)(2 * D::WQ + b * 32 + hf * 16 + 8), qpv + 8);
         }
         const uint32_t aB = sA + b * 4 * A_TILE_STD;
 #pragma unroll
@@ -730,9 +752,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
                 } else {
                     const bool first = (s % TC_FLUSH) == 0;
                     if (warp == 0)
-                        issue_stage_group<K, 0>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, first);
+                        issue_stage_group<K, 0>(tmem, d * D::WQ, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, first);
                     else
-                        issue_stage_group<K, 1>(tmem, d * D::NT, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, first);
+                        issue_stage_group<K, 1>(tmem, d * D::WQ, aB, A_TILE_STD, LBO_STD, SBO_STD, sR + slot * GBM, first);
                     commit_stage(sy, s, ns, b);
                 }
             }
