@@ -56,6 +56,8 @@ def parse(argv=None):
     ap.add_argument("--em-iters", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-full", action="store_true",
+                    help="run the plain FP64 fit to convergence (minutes) and compare it with the chosen fit")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--cpu-slice-blocks", type=int, default=0)
@@ -352,13 +354,29 @@ def run_ours(args, world, rank, local):
         t0 = time.time()
         dp.qn_iteration()
         t_it = time.time() - t0
-        dp.close()
         # init_em evaluates the log-likelihood after its last step only
         est = args.em_iters * (t_em - t_ll) + t_ll + iters * t_it
         line["plain_fp64"] = {"s_per_em_iter": t_em, "s_per_loglik": t_ll, "s_per_outer_iter": t_it,
                               "est_s_to_converge": est, "est_speedup_chosen_vs_plain": est / (ms / 1e3),
                               "note": "extrapolated: measured EM and outer-iteration times x the chosen "
                                       "fit's iteration counts"}
+        if args.plain_full:
+            # the plain fit to convergence from the same start, against the
+            # chosen fit's result (ll relative, Q and P largest absolute)
+            q_c, p_c = d.get_qp()
+            dp.set_qp_device(q0_dev.data_ptr(), p0_dev.data_ptr())
+            torch.cuda.synchronize()
+            t0 = time.time()
+            pinfo = dp.fit(n_iter=args.n_iter, rtol=args.rtol, em_iters=args.em_iters)
+            t_full = time.time() - t0
+            q_f, p_f = dp.get_qp()
+            line["plain_fp64"].update({
+                "measured_s_to_converge": t_full, "measured_outer_iters": pinfo["iters"], "ll": pinfo["ll"],
+                "measured_speedup_chosen_vs_plain": t_full / (ms / 1e3),
+                "chosen_vs_plain": {"ll_rel_diff": abs(ll - pinfo["ll"]) / abs(pinfo["ll"]),
+                                    "q_max_abs_diff": float(np.abs(q_c - q_f).max()),
+                                    "p_max_abs_diff": float(np.abs(p_c - p_f).max())}})
+        dp.close()
 
     # end to end through the public API from host buffers
     if not args.no_e2e:
