@@ -364,7 +364,8 @@ int qn_iteration(hx_ctx* c) {
     HX_ST(update_p(c, true));
     HX_ST(loglik_to_slot(c, qof(c->xn2), pof(c, c->xn2), S_LL_BASIC));
     HX_LAUNCH(HX_KIND_QN, 3,
-              launch_qn(c->nx, c->x, c->xn, c->xn2, c->U, c->V, c->Qs, c->part_qn, c->coef, c->xt, c->slots, c->st));
+              launch_qn(c->nx, c->x, c->xn, c->xn2, c->U, c->V, c->Qs, c->part_qn, c->coef, c->xt, c->slots, c->st,
+                        c->lo.mode));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_p(pof(c, c->xt), nullptr, c->K, c->J, c->eps, pof(c, c->xt), c->st));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_q(qof(c->xt), nullptr, c->K, c->I, c->eps, qof(c->xt), c->st));
     HX_ST(loglik_to_slot(c, qof(c->xt), pof(c, c->xt), S_LL_QN));
@@ -442,7 +443,7 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     if (Sp_max > 1) HX_ST(dalloc(c, &c->part_p, (size_t)Sp_max * NVmax * 4 * J));
     HX_ST(dalloc(c, &c->part_ll, (size_t)std::max<int64_t>((c->Ipad / ACC_THREADS) * c->S_q,
                                                             (int64_t)loglik_f32x2_blocks(c->Ipad, K) * c->S_ll)));
-    HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (2 * HX_QMAX * HX_QMAX + HX_QMAX)));
+    HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (3 * HX_QMAX * HX_QMAX + 2 * HX_QMAX)));
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));
     if (c->tc) HX_ST(dalloc(c, &c->img, tc_image_bytes(K, I, J)));
@@ -520,12 +521,14 @@ int hx_loop_opts_default(hx_loop_opts* o) {
     o->fix_p = 0;
     o->guarantee_increase = 0;
     o->penalty = -1;
+    o->mode = 0;
     return HX_OK;
 }
 
 int hx_set_loop_opts(hx_ctx* c, const hx_loop_opts* o) {
     if (!c || !o) return HX_EINVAL;
     if (o->penalty < -1 || o->penalty > 1) return fail(c, HX_EINVAL, "penalty must be -1, 0 or 1");
+    if (o->mode < 0 || o->mode > 1) return fail(c, HX_EINVAL, "mode must be 0 (ZAL) or 1 (LBQN)");
     c->lo = *o;
     return HX_OK;
 }
@@ -791,7 +794,7 @@ int hx_zal(hx_ctx* c, const double* x, const double* x_next, const double* x_nex
     double* dU = t.get<double>(c, (size_t)n * Qs, &st);
     double* dV = t.get<double>(c, (size_t)n * Qs, &st);
     double* dxt = t.get<double>(c, n, &st);
-    double* part = t.get<double>(c, (size_t)qn_dots_blocks(n) * (2 * HX_QMAX * HX_QMAX + HX_QMAX), &st);
+    double* part = t.get<double>(c, (size_t)qn_dots_blocks(n) * (3 * HX_QMAX * HX_QMAX + 2 * HX_QMAX), &st);
     double* coef = t.get<double>(c, HX_QMAX, &st);
     double* slots = t.get<double>(c, HX_NSLOT, &st);
     if (st != HX_OK) return st;

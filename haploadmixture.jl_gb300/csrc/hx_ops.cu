@@ -624,11 +624,13 @@ k_qp_p(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
 // ------------------------------------------------------------------ ZAL QN
 constexpr int QN_THREADS = 256;
 
-template <int QS>
+// Secant-pair update and the dot products of the QN point: UtU (full), UtV,
+// Utd with d = x - x_next, and for LB (the LBQN step) also VtV and Vtd.
+template <int QS, bool LB>
 __global__ void __launch_bounds__(QN_THREADS)
 k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn, const double* __restrict__ xn2,
           double* __restrict__ U, double* __restrict__ V, const double* __restrict__ slots, double* __restrict__ part) {
-    constexpr int NV = QS * QS * 2 + QS;   // UtU (full), UtV, Utd
+    constexpr int NV = QS * QS * 2 + QS + (LB ? QS * QS + QS : 0);
     __shared__ double red[QN_THREADS / 32][NV];
     const int it = (int)slots[S_ITER];
     const int col = (it > 0 ? it - 1 : 0) % QS;
@@ -653,8 +655,10 @@ k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn
             for (int s = 0; s < QS; ++s) {
                 acc[r * QS + s] += u[r] * u[s];
                 acc[QS * QS + r * QS + s] += u[r] * v[s];
+                if (LB) acc[2 * QS * QS + QS + r * QS + s] += v[r] * v[s];
             }
             acc[2 * QS * QS + r] += u[r] * dxa;
+            if (LB) acc[3 * QS * QS + QS + r] += v[r] * dxa;
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -675,10 +679,13 @@ k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn
 // Sums the block partials in block order, then solves (U'U - U'V) c = U'(x - x_next)
 // on the first m = min(iter, QS) secant pairs (Gaussian elimination with
 // partial pivoting, as Julia's `\`).
+// The Q x Q system of the QN point, solved as Julia's `\` (Gaussian
+// elimination with partial pivoting): ZAL (lb = 0) (U'U - U'V) c = U'd;
+// LBQN (lb = 1) (U-V)'(U-V) c = (U-V)'d.
 __global__ void k_qn_solve(const double* __restrict__ part, int nblk, int QS, const double* __restrict__ slots,
-                           double* __restrict__ coef) {
-    __shared__ double tot[2 * HX_QMAX_DEV * HX_QMAX_DEV + HX_QMAX_DEV];
-    const int NV = QS * QS * 2 + QS;
+                           double* __restrict__ coef, int lb) {
+    __shared__ double tot[3 * HX_QMAX_DEV * HX_QMAX_DEV + 2 * HX_QMAX_DEV];
+    const int NV = QS * QS * 2 + QS + (lb ? QS * QS + QS : 0);
     for (int v = threadIdx.x; v < NV; v += blockDim.x) {
         double s = 0.0;
         for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * NV + v];
@@ -689,9 +696,14 @@ __global__ void k_qn_solve(const double* __restrict__ part, int nblk, int QS, co
     const int it = (int)slots[S_ITER];
     const int m = it < QS ? it : QS;
     double A[HX_QMAX_DEV * HX_QMAX_DEV], b[HX_QMAX_DEV];
+    const double* VtV = tot + 2 * QS * QS + QS;
+    const double* Vtd = tot + 3 * QS * QS + QS;
     for (int r = 0; r < m; ++r) {
-        for (int s = 0; s < m; ++s) A[r + m * s] = tot[r * QS + s] - tot[QS * QS + r * QS + s];
-        b[r] = tot[2 * QS * QS + r];
+        for (int s = 0; s < m; ++s) {
+            const double uu = tot[r * QS + s], uv = tot[QS * QS + r * QS + s];
+            A[r + m * s] = lb ? ((uu - uv) - tot[QS * QS + s * QS + r]) + VtV[r * QS + s] : uu - uv;
+        }
+        b[r] = lb ? tot[2 * QS * QS + r] - Vtd[r] : tot[2 * QS * QS + r];
     }
     for (int c = 0; c < m; ++c) {
         int piv = c;
@@ -889,20 +901,21 @@ int qn_dots_blocks(int64_t n) {
     return (int)(b < 1 ? 1 : (b > 1216 ? 1216 : b));
 }
 cudaError_t launch_qn(int64_t n, const double* x, const double* xn, const double* xn2, double* U, double* V, int Qs,
-                      double* part, double* coef, double* xt, double* slots, cudaStream_t st) {
+                      double* part, double* coef, double* xt, double* slots, cudaStream_t st, int mode) {
     const int nb = qn_dots_blocks(n);
+#define HX_QN(QQ)                                                                                       \
+    case QQ:                                                                                            \
+        if (mode == 1) k_qn_dots<QQ, true><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part);  \
+        else k_qn_dots<QQ, false><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part);          \
+        break;
     switch (Qs) {
-        case 1: k_qn_dots<1><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part); break;
-        case 2: k_qn_dots<2><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part); break;
-        case 3: k_qn_dots<3><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part); break;
-        case 4: k_qn_dots<4><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part); break;
-        case 5: k_qn_dots<5><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part); break;
-        case 6: k_qn_dots<6><<<nb, QN_THREADS, 0, st>>>(n, x, xn, xn2, U, V, slots, part); break;
+        HX_QN(1) HX_QN(2) HX_QN(3) HX_QN(4) HX_QN(5) HX_QN(6)
         default: return cudaErrorInvalidValue;
     }
+#undef HX_QN
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_qn_solve<<<1, 128, 0, st>>>(part, nb, Qs, slots, coef);
+    k_qn_solve<<<1, 128, 0, st>>>(part, nb, Qs, slots, coef, mode == 1 ? 1 : 0);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_qn_apply<<<nblk(n, 256) < 2432 ? nblk(n, 256) : 2432, 256, 0, st>>>(n, xn, V, Qs, coef, xt);

@@ -103,10 +103,11 @@ cudaError_t launch_qp_q(int K, int64_t n, const double* XtX, const double* Xtz, 
 // eq: the equality form (K equalities per block, rho and ws unused)
 cudaError_t launch_qp_p(int K, int64_t n, const double* XtX, const double* Xtz, const double* p, double rho,
                         double* pdiff, double* slots, int8_t* ws, cudaStream_t st, bool eq = false);
-// ZAL quasi-Newton
+// quasi-Newton point (ZAL or LBQN)
 int qn_dots_blocks(int64_t n);
+// mode 0: ZAL, 1: LBQN (the limited-memory Broyden step)
 cudaError_t launch_qn(int64_t n, const double* x, const double* xn, const double* xn2, double* U, double* V,
-                      int Qs, double* part, double* coef, double* xt, double* slots, cudaStream_t st);
+                      int Qs, double* part, double* coef, double* xt, double* slots, cudaStream_t st, int mode = 0);
 // outer-iteration bookkeeping
 cudaError_t launch_iter_begin(double* slots, cudaStream_t st);
 cudaError_t launch_accept(int64_t n, double* x, const double* xt, const double* xn2, double* slots,

@@ -27,7 +27,8 @@ class HxOpts(C.Structure):
 
 class HxLoopOpts(C.Structure):
     _fields_ = [("fix_q", C.c_int32), ("fix_p", C.c_int32), ("guarantee_increase", C.c_int32),
-                ("penalty", C.c_int32)]
+                ("penalty", C.c_int32),
+                ("mode", C.c_int32)]
 
 
 class HxIterInfo(C.Structure):

@@ -172,14 +172,16 @@ class GB300Admix:
     # -- launch accounting
     KINDS = ("accum_q", "accum_p", "loglik", "qp_q", "qp_p", "qn", "other")
 
-    def set_loop_opts(self, fix_q=False, fix_p=False, guarantee_increase=False, penalty=None):
+    def set_loop_opts(self, fix_q=False, fix_p=False, guarantee_increase=False, penalty=None, mode="ZAL"):
         """admixture_qn!/init_em! keyword options (src/algorithms_outer.jl:1-3, 38-41);
         penalty None is the reference default (P penalty form, Q equality form),
-        True the penalty form for both steps, False the equality form for both."""
+        True the penalty form for both steps, False the equality form for both;
+        mode "ZAL" (default) or "LBQN" selects admixture_qn!'s quasi-Newton step."""
         o = _lib.HxLoopOpts()
         self._ck(self.lib.hx_loop_opts_default(C.byref(o)))
         o.fix_q, o.fix_p, o.guarantee_increase = int(fix_q), int(fix_p), int(guarantee_increase)
         o.penalty = -1 if penalty is None else int(bool(penalty))
+        o.mode = {"ZAL": 0, "LBQN": 1}[mode]
         self._ck(self.lib.hx_set_loop_opts(self._h, C.byref(o)))
 
     def set_profiling(self, on=True):

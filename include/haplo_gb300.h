@@ -90,11 +90,14 @@ typedef struct hx_loop_opts {
                                     1: penalty form for both (rho * 1 1' on each Q block);
                                     0: equality form for both (P: sum_h d[k,h] = 0 for every k,
                                        src/algorithms_inner.jl:307-310) */
+    int32_t mode;                /* admixture_qn!'s mode (src/algorithms_outer.jl:128-138): 0 = :ZAL
+                                    (default), 1 = :LBQN, the limited-memory Broyden step
+                                    x_next - V ((U-V)'(U-V))^-1 (U-V)'(x - x_next) */
 } hx_loop_opts;
 
 /* Defaults: precision FP64, device 0, Qsec 3, rho 1e7, pseudocount 1e-5. */
 int hx_opts_default(hx_opts* opts);
-/* Defaults: no fixed factor, no step control, penalty -1. */
+/* Defaults: no fixed factor, no step control, penalty -1, mode 0 (ZAL). */
 int hx_loop_opts_default(hx_loop_opts* opts);
 int hx_set_loop_opts(hx_ctx* ctx, const hx_loop_opts* opts);
 const char* hx_status_string(int status);

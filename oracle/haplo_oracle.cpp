@@ -766,11 +766,20 @@ int orc_update_p(const uint8_t* bed, int64_t bps, int64_t I, int64_t J, int K, c
     return f;
 }
 
-// OpenADMIXTURE.update_UV! + update_QN! as called at src/algorithms_outer.jl:
-// 129-133: column c = (it-1) mod Qs of U/V gets x_next - x and x_next2 - x_next;
-// with m = min(it, Qs) columns, x_tmp = x_next - V (U'U - U'V)^{-1} U'(x - x_next).
-void orc_zal(int64_t n, const double* x, const double* x_next, const double* x_next2, double* U, double* V,
-             int Qs, int it, double* x_tmp) {
+// The quasi-Newton point of admixture_qn! (src/algorithms_outer.jl:128-138):
+// column c = (it-1) mod Qs of U/V gets x_next - x and x_next2 - x_next; with
+// m = min(it, Qs) columns and d = x - x_next,
+//   mode 0, ZAL (update_UV!/update_QN!, Zhou, Alexander & Lange 2011):
+//     x_tmp = x_next - V (U'U - U'V)^{-1} U' d   (the multi-secant "good"
+//     Broyden inverse with H0 = -I, secant pairs s = u, y = v - u);
+//   mode 1, LBQN (update_UV_LBQN!/update_QN_LBQN!, the limited-memory Broyden
+//     method of Agarwal & Xu): the multi-secant "bad" Broyden inverse
+//     H = -I + V (Y'Y)^{-1} Y', Y = V - U, which satisfies H Y = U, giving
+//     x_tmp = x_next - V ((U-V)'(U-V))^{-1} (U-V)' d.
+// OpenADMIXTURE's LBQN code is not available here: this restates the
+// published method, so its trajectory is not pinned to the reference's.
+void qn_point(int64_t n, const double* x, const double* x_next, const double* x_next2, double* U, double* V,
+              int Qs, int it, int mode, double* x_tmp) {
     int c = (it - 1) % Qs;
     for (int64_t a = 0; a < n; ++a) {
         U[a + n * c] = x_next[a] - x[a];
@@ -780,13 +789,21 @@ void orc_zal(int64_t n, const double* x, const double* x_next, const double* x_n
     std::vector<double> A(m * m), b(m);
     for (int r = 0; r < m; ++r) {
         for (int s = 0; s < m; ++s) {
-            double uu = 0.0, uv = 0.0;
-            for (int64_t a = 0; a < n; ++a) { uu += U[a + n * r] * U[a + n * s]; uv += U[a + n * r] * V[a + n * s]; }
-            A[r + m * s] = uu - uv;
+            double uu = 0.0, uv = 0.0, vu = 0.0, vv = 0.0;
+            for (int64_t a = 0; a < n; ++a) {
+                uu += U[a + n * r] * U[a + n * s];
+                uv += U[a + n * r] * V[a + n * s];
+                vu += V[a + n * r] * U[a + n * s];
+                vv += V[a + n * r] * V[a + n * s];
+            }
+            A[r + m * s] = mode == 1 ? ((uu - uv) - vu) + vv : uu - uv;
         }
-        double t = 0.0;
-        for (int64_t a = 0; a < n; ++a) t += U[a + n * r] * (x[a] - x_next[a]);
-        b[r] = t;
+        double t = 0.0, tv = 0.0;
+        for (int64_t a = 0; a < n; ++a) {
+            t += U[a + n * r] * (x[a] - x_next[a]);
+            tv += V[a + n * r] * (x[a] - x_next[a]);
+        }
+        b[r] = mode == 1 ? t - tv : t;
     }
     solve_small(m, A, b);
     for (int64_t a = 0; a < n; ++a) {
@@ -794,6 +811,14 @@ void orc_zal(int64_t n, const double* x, const double* x_next, const double* x_n
         for (int r = 0; r < m; ++r) t += V[a + n * r] * b[r];
         x_tmp[a] = x_next[a] - t;
     }
+}
+void orc_zal(int64_t n, const double* x, const double* x_next, const double* x_next2, double* U, double* V,
+             int Qs, int it, double* x_tmp) {
+    qn_point(n, x, x_next, x_next2, U, V, Qs, it, 0, x_tmp);
+}
+void orc_qn(int64_t n, const double* x, const double* x_next, const double* x_next2, double* U, double* V,
+            int Qs, int it, int mode, double* x_tmp) {
+    qn_point(n, x, x_next, x_next2, U, V, Qs, it, mode, x_tmp);
 }
 
 // Loop options of admixture_qn!/init_em! (src/algorithms_outer.jl:1-3, 38-41):
@@ -851,7 +876,7 @@ void update_p_opts(const Dims& D, const double* q, const double* p, double* p_ne
 }  // namespace
 
 // src/algorithms_outer.jl:1-22 (init_em!) followed by :38-172 (admixture_qn!,
-// mode = :ZAL) with the loop options above.  x (K x (I+4J)) holds the initial
+// mode = :ZAL, or :LBQN with mode 1) with the loop options above.  x (K x (I+4J)) holds the initial
 // [q | p] and receives the final one; trace (optional, n_iter entries)
 // receives ll after every outer iteration.  EM with fix_q / fix_p keeps that
 // factor unchanged (the reference's em! rescales a fixed q before projecting
@@ -859,7 +884,7 @@ void update_p_opts(const Dims& D, const double* q, const double* p, double* p_ne
 // restated).  Returns 0.
 int orc_fit_ex(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J, int K, int Qs, double* x,
                int n_iter, double rtol, int em_iters, double rho, int nthreads, double* ll_out, int* iters_out,
-               double* trace, int fix_q, int fix_p, int guarantee_increase, int penalty) {
+               double* trace, int fix_q, int fix_p, int guarantee_increase, int penalty, int mode) {
     LoopOpts o;
     o.fix_q = fix_q; o.fix_p = fix_p; o.gi = guarantee_increase; o.penalty = penalty;
     Dims D{bed, bps, nsnp, I, J, K};
@@ -893,7 +918,7 @@ int orc_fit_ex(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t
         update_q_opts(D, qn, pn, qn2, o, rho, ll_tmp, nthreads);
         update_p_opts(D, qn2, pn, pn2, o, rho, ll_tmp, nthreads);
         double ll_basic = loglik(D, qn2, pn2, 2, nthreads);
-        orc_zal(n, x, xn.data(), xn2.data(), U.data(), V.data(), Qs, it, xt.data());
+        qn_point(n, x, xn.data(), xn2.data(), U.data(), V.data(), Qs, it, mode, xt.data());
         project_p_all(xt.data() + (int64_t)K * I, K, J, 1e-5, nthreads);
         project_q_all(xt.data(), K, I, 1e-5, nthreads);
         double ll_qn = loglik(D, xt.data(), xt.data() + (int64_t)K * I, 2, nthreads);
@@ -918,7 +943,7 @@ int orc_fit(const uint8_t* bed, int64_t bps, int64_t nsnp, int64_t I, int64_t J,
             int n_iter, double rtol, int em_iters, double rho, int nthreads, double* ll_out, int* iters_out,
             double* trace) {
     return orc_fit_ex(bed, bps, nsnp, I, J, K, Qs, x, n_iter, rtol, em_iters, rho, nthreads, ll_out, iters_out,
-                      trace, 0, 0, 0, -1);
+                      trace, 0, 0, 0, -1, 0);
 }
 
 // ---------------------------------------------------------------- synthetic

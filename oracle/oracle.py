@@ -52,7 +52,8 @@ def _load():
             "orc_zal": (None, [I64, P, P, P, P, P, I32, I32, P]),
             "orc_fit": (I32, [P, I64, I64, I64, I64, I32, I32, P, I32, Dd, I32, Dd, I32, P, P, P]),
             "orc_fit_ex": (I32, [P, I64, I64, I64, I64, I32, I32, P, I32, Dd, I32, Dd, I32, P, P, P,
-                                 I32, I32, I32, I32]),
+                                 I32, I32, I32, I32, I32]),
+            "orc_qn": (None, [I64, P, P, P, P, P, I32, I32, I32, P]),
             "orc_synth": (None, [C.c_uint64, I64, I64, I32, P, P, Dd, P, I32]),
         }
         for name, (res, args) in sig.items():
@@ -222,11 +223,24 @@ def zal(x, x_next, x_next2, U, V, it):
     return xt, U, V
 
 
+def qn(x, x_next, x_next2, U, V, it, mode="ZAL"):
+    """The quasi-Newton point of admixture_qn!: mode "ZAL" or "LBQN"."""
+    n = x.size
+    x, x_next, x_next2 = (np.ascontiguousarray(np.ravel(a, order="F"), dtype=np.float64) for a in (x, x_next, x_next2))
+    U = np.array(U, dtype=np.float64, order="F", copy=True)
+    V = np.array(V, dtype=np.float64, order="F", copy=True)
+    xt = np.empty(n)
+    _load().orc_qn(n, _p(x), _p(x_next), _p(x_next2), _p(U), _p(V), U.shape[1], it, {"ZAL": 0, "LBQN": 1}[mode],
+                   _p(xt))
+    return xt, U, V
+
+
 def fit(b, K, q, p, n_iter=1000, rtol=1e-7, em_iters=5, Qs=3, rho=1e7, threads=None, fix_q=False, fix_p=False,
-        guarantee_increase=False, penalty=None):
+        guarantee_increase=False, penalty=None, mode="ZAL"):
     """init_em! + admixture_qn! on the CPU; returns (q, p, ll, iters, trace).
     penalty None is the reference default (P penalty form, Q equality form);
-    True uses the penalty form for both, False the equality form for both."""
+    True uses the penalty form for both, False the equality form for both.
+    mode: "ZAL" (default) or "LBQN", the quasi-Newton step of admixture_qn!."""
     q, p = _F(q, (K, b.I)), _F(p, (K, 4 * b.J))
     x = np.asfortranarray(np.hstack([q, p]))
     ll = C.c_double()
@@ -235,7 +249,7 @@ def fit(b, K, q, p, n_iter=1000, rtol=1e-7, em_iters=5, Qs=3, rho=1e7, threads=N
     pen = -1 if penalty is None else int(bool(penalty))
     r = _load().orc_fit_ex(b.ptr, b.bps, b.n_snp, b.I, b.J, K, Qs, _p(x), n_iter, rtol, em_iters, rho,
                            threads or nthreads(), C.byref(ll), C.byref(iters), _p(trace), int(fix_q), int(fix_p),
-                           int(guarantee_increase), pen)
+                           int(guarantee_increase), pen, {"ZAL": 0, "LBQN": 1}[mode])
     return (np.asfortranarray(x[:, :b.I]), np.asfortranarray(x[:, b.I:]), ll.value, iters.value,
             trace[:iters.value])
 

@@ -218,7 +218,7 @@ def test_errors_are_status_codes(hx, coh):
 
 
 @pytest.mark.parametrize("opts", [dict(fix_q=True), dict(fix_p=True), dict(guarantee_increase=True),
-                                  dict(penalty=True), dict(penalty=False)])
+                                  dict(penalty=True), dict(penalty=False), dict(mode="LBQN")])
 def test_loop_options_match_oracle_fp64(hx, O, opts):
     # admixture_qn!/init_em! keywords (src/algorithms_outer.jl:1-3, 38-41)
     c = small_cohort(240, 120, 3, seed=33, alpha=0.5, miss=0.01)

@@ -255,6 +255,38 @@ def test_zal_formula(O):
         U, V = U2, V2
 
 
+def test_lbqn_point_is_the_bad_broyden_step(O):
+    # mode LBQN: the multi-secant "bad" Broyden inverse H = -I + V (Y'Y)^-1 Y',
+    # Y = V - U, satisfies H Y = U, and the point is x - H (F(x) - x)
+    rng = np.random.default_rng(6)
+    n, Qs = 40, 3
+    U = rng.normal(size=(n, Qs))
+    V = rng.normal(size=(n, Qs))
+    for it in (1, 2, 3, 4, 5):
+        x, xn, xn2 = rng.normal(size=(3, n))
+        xt, U2, V2 = O.qn(x, xn, xn2, U, V, it, mode="LBQN")
+        c = (it - 1) % Qs
+        np.testing.assert_allclose(U2[:, c], xn - x)
+        np.testing.assert_allclose(V2[:, c], xn2 - xn)
+        m = min(it, Qs)
+        Um, Vm = U2[:, :m], V2[:, :m]
+        Y = Vm - Um
+        H = -np.eye(n) + Vm @ np.linalg.solve(Y.T @ Y, Y.T)
+        np.testing.assert_allclose(H @ Y, Um, atol=1e-10)
+        np.testing.assert_allclose(xt, x - H @ (xn - x), rtol=1e-9, atol=1e-10)
+        zt, _, _ = O.qn(x, xn, xn2, U, V, it, mode="ZAL")
+        np.testing.assert_allclose(zt, O.zal(x, xn, xn2, U, V, it)[0], rtol=0, atol=0)
+        U, V = U2, V2
+
+
+def test_lbqn_fit_reaches_the_zal_optimum(O, loop_case):
+    c, b, q0, p0 = loop_case
+    _, _, ll_z, _, _ = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3)
+    q, p, ll_l, it, trace = O.fit(b, 3, q0, p0, n_iter=400, rtol=1e-12, em_iters=3, mode="LBQN")
+    assert ll_l == pytest.approx(ll_z, rel=1e-7)
+    assert np.all(np.diff(trace) >= -1e-9 * np.abs(trace[1:]))   # each iteration keeps the better point
+
+
 def test_fit_beats_truth_and_converges(O):
     c = small_cohort(400, 300, 3, seed=21, alpha=0.5, miss=0.01)
     b = O.Bed(c["bed"], c["I"], c["J"])
