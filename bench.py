@@ -14,8 +14,12 @@ L2 (129 MB), so no flush is needed between steps.
           the H2D copy of the .bed matrix and initial Q/P and the D2H of the
           fitted Q/P and log-likelihood
   roofline : dominant kernel, algorithmic bytes per launch / CUDA-event time
-  cpu_baseline : CPU oracle (C++ restatement, all host cores) on a bounded
-          slice, extrapolated to the full fit (labelled)
+  plain_fp64 : the plain FP64 GPU method fitted to convergence once from the
+          same start (the metric's comparison), with the chosen fit's
+          log-likelihood and Q/P differences against it
+  cpu_baseline : CPU oracle (C++ restatement, all host cores): each piece of
+          the fit timed on a bounded slice or at full size, summed with the
+          fit's iteration counts (extrapolated, labelled)
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -35,8 +39,9 @@ for _p in (ROOT, os.path.join(ROOT, "haploadmixture.jl_gb300")):
         sys.path.insert(0, _p)
 
 METRIC = "s to converge (rel Δloglik<1e-8), I=1e5×2e5 SNPs K=8: chosen vs plain GPU"
-# outer iterations of the C3 fit measured on GB300 (26 at rtol 1e-8); used
-# only to extrapolate the CPU reference arm, whose full fit takes hours
+# outer iterations of the I=1e5, J=1e5, K=8 fit measured on GB300 (26 at rtol
+# 1e-8); used only to extrapolate the CPU reference arm, whose full fit takes
+# hours
 REF_ITERS_DEFAULT = 26
 
 
@@ -56,8 +61,9 @@ def parse(argv=None):
     ap.add_argument("--em-iters", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--plain-full", action="store_true",
-                    help="run the plain FP64 fit to convergence (minutes) and compare it with the chosen fit")
+    ap.add_argument("--plain-estimate", action="store_true",
+                    help="time one EM and one outer iteration of the plain FP64 method instead of fitting it "
+                         "to convergence (the default, about 11 minutes at I=1e5, J=1e5, K=8)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--cpu-slice-blocks", type=int, default=0)
@@ -148,9 +154,9 @@ def pass_flops(I, J, K):
 
 
 # DRAM bytes (read + write) per (individual, block) pair of the tensor-core
-# Hessian passes, from one-pass ncu captures of one launch each at I=100,000,
-# J=100,000, K=8 (profiles/k_accum_tc_c3_dram.md): P 5.65 GB, Q 5.83 GB per
-# launch over 1e10 pairs.
+# Hessian passes, from one-pass ncu captures (dram__bytes_read.sum +
+# dram__bytes_write.sum) of one launch each at I=100,000, J=100,000, K=8:
+# P 5.65 GB, Q 5.83 GB per launch over 1e10 pairs.
 TRAFFIC_PER_PAIR = {"accum_q": 0.592, "accum_p": 0.588}
 
 
@@ -164,28 +170,76 @@ def load_config(args):
     return synth.config(args.config, I=args.I, J=args.J, K=args.K)
 
 
-def cpu_oracle_sample(cfg, slice_blocks, threads):
-    """Times the CPU oracle on an I x slice_blocks slice: one EM step and one
-    outer QN iteration (4 accumulations + QPs + 2 log-likelihoods + ZAL)."""
+def cpu_info():
+    """Host cores and CPU model, as nproc and lscpu report them."""
+    info = {"nproc": os.cpu_count() or 1}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            k, _, v = ln.partition(":")
+            if k.strip() in ("Model name", "Architecture", "Socket(s)", "Core(s) per socket", "Thread(s) per core"):
+                info[k.strip()] = v.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
+
+
+def cpu_components(cfg, slice_blocks, j0, threads, seed):
+    """Seconds of the CPU oracle's pieces of the fit, timed on an I x
+    slice_blocks slice of the cohort (blocks j0 .. j0+slice_blocks-1 of P) for
+    the work that grows with J, and at full size for the rest:
+      per slice: em (both gradient-only passes), ll, accum_q, accum_p (Hessian
+        passes), qp_p (per-block QPs), proj_p (quartet projections);
+      full size: qp_q (the I per-individual QPs), proj_q, qn (ZAL point on
+        vectors of K (I + 4J))."""
     from oracle import oracle as O
     from haplo_gb300 import synth
-    from haplo_gb300.admix import random_init
-    I, K = cfg["I"], cfg["K"]
+    I, J, K = cfg["I"], cfg["J"], cfg["K"]
     Js = slice_blocks
-    Q = cfg["Q"]
-    P = cfg["P"][:, :4 * Js]
-    cq, cp = synth.cumulative(Q, P)
-    bed = O.synth(cfg["seed"], I, Js, cq, cp, cfg["miss"], threads=threads)
+    P = cfg["P"][:, 4 * j0:4 * (j0 + Js)]
+    cq, cp = synth.cumulative(cfg["Q"], P)
+    bed = O.synth(cfg["seed"] + j0, I, Js, cq, cp, cfg["miss"], threads=threads)
     b = O.Bed(bed, I, Js)
-    q0, p0 = random_init(I, Js, K, np.random.default_rng(7))
-    t0 = time.time()
-    q1, p1 = O.em_step(b, K, q0, p0, threads=threads)
-    O.loglik(b, K, q1, p1, threads=threads)
-    t_em = time.time() - t0
-    t0 = time.time()
-    O.fit(b, K, q1, p1, n_iter=1, rtol=0.0, em_iters=0, threads=threads)
-    t_it = time.time() - t0
-    return t_em, t_it
+    rng = np.random.default_rng(seed)
+    x = rng.random((K, I + 4 * Js))
+    q = np.asfortranarray(x[:, :I] / x[:, :I].sum(axis=0, keepdims=True))
+    p4 = x[:, I:].reshape(K, Js, 4)
+    p = np.asfortranarray((p4 / p4.sum(axis=2, keepdims=True)).reshape(K, 4 * Js))
+    t = {}
+
+    def timed(name, f, *a, **kw):
+        t0 = time.perf_counter()
+        r = f(*a, **kw)
+        t[name] = time.perf_counter() - t0
+        return r
+
+    timed("em", O.em_accum, b, K, q, p, threads=threads)
+    timed("ll", O.loglik, b, K, q, p, threads=threads)
+    XtXq, Xtzq = timed("accum_q", O.accum_q, b, K, q, p, threads=threads)
+    XtXp, Xtzp = timed("accum_p", O.accum_p, b, K, q, p, threads=threads)
+    timed("qp_p", O.qp_p, XtXp, Xtzp, p, threads=threads)
+    timed("proj_p", O.project_p, p)
+    timed("qp_q", O.qp_q, XtXq, Xtzq, q, threads=threads)
+    timed("proj_q", O.project_q, q)
+    n = K * (I + 4 * J)
+    v = rng.random((3, n))
+    U, V = np.zeros((n, 3)), np.zeros((n, 3))
+    for it in (1, 2, 3):
+        timed("qn", O.zal, v[0], v[1], v[2], U, V, it)
+    return t
+
+
+def cpu_fit_model(t, J, slice_blocks, em_iters, outer_iters):
+    """Seconds of the reference's fit from per-piece times (cpu_components):
+    the slice pieces scaled by J / slice_blocks, the rest as measured.
+      EM iteration (src/algorithms_outer.jl:4-18): em + ll + projections;
+      outer iteration (src/algorithms_outer.jl:65-171): 2 x (accum_q + qp_q +
+      proj_q) + 2 x (accum_p + qp_p + proj_p) + 2 ll + qn + proj of the QN point."""
+    s = J / float(slice_blocks)
+    em = (t["em"] + t["ll"] + t["proj_p"]) * s + t["proj_q"]
+    outer = (2 * (t["accum_q"] + t["accum_p"] + t["qp_p"] + t["proj_p"]) + 2 * t["ll"] + t["proj_p"]) * s \
+        + 2 * (t["qp_q"] + t["proj_q"]) + t["qn"] + t["proj_q"]
+    return em_iters * em + outer_iters * outer, em, outer
 
 
 def dist_setup(args):
@@ -216,32 +270,82 @@ def barrier(world):
         dist.barrier()
 
 
+def bench_config(args, cfg):
+    """The workload description both arms print as "config"."""
+    return {"workload": workload(args.config, cfg), "rtol": args.rtol, "em_iters": args.em_iters,
+            "n_iter_cap": args.n_iter,
+            "l2": "inputs (class words: I*J/2 bytes, 5 GB at I=1e5, J=1e5) larger than L2; no flush"}
+
+
 def run_reference(args, world, rank):
     """CPU reference arm: the oracle port (C++ restatement of the reference's
-    CPU loops, all host threads) on bounded slices of the workload."""
+    CPU loops, all host threads).  Each step times the fit's pieces on an
+    I x slice_blocks slice of the blocks (a different slice each step) and at
+    full size for the I-only work, then adds them up with the fit's iteration
+    counts (cpu_fit_model)."""
     if rank != 0:
         return
     cfg = load_config(args)
     threads = os.cpu_count() or 1
-    Js = args.cpu_slice_blocks or 200
-    vals = []
+    Js = min(args.cpu_slice_blocks or 1000, cfg["J"])
+    vals, sample_s = [], []
     for s in range(args.warmup + args.steps):
-        t_em, t_it = cpu_oracle_sample(cfg, Js, threads)
-        scale = cfg["J"] / Js
-        v = (args.em_iters * t_em + args.ref_iters * t_it) * scale
+        j0 = (s * Js) % max(1, cfg["J"] - Js + 1)
+        t0 = time.perf_counter()
+        t = cpu_components(cfg, Js, j0, threads, seed=cfg["seed"] + s)
+        sample_s.append(time.perf_counter() - t0)
+        v, _, _ = cpu_fit_model(t, cfg["J"], Js, args.em_iters, args.ref_iters)
         if s >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
-    sample = ("oracle port on I=%d x %d-block slices (%.2f%% of the blocks): %d EM steps + %d outer "
-              "iterations, per-block time scaled by J/%d; iteration count %d from the GB300 fit (extrapolated)"
-              % (cfg["I"], Js, 100.0 * Js / cfg["J"], args.em_iters, args.ref_iters, Js, args.ref_iters))
+    sample = ("oracle port, %d host threads: per step, the J-proportional pieces (EM and Hessian passes, "
+              "log-likelihood, per-block QPs and projections) timed on an I=%d x %d-block slice (%.1f%% of "
+              "the blocks; a different slice each step) and scaled by J/%d, the I-only pieces (per-individual "
+              "QPs, projections) and the ZAL point timed at full size; summed with %d EM + %d outer iterations "
+              "(the GB300 fit's count): extrapolated, %.1f s of CPU work per step"
+              % (threads, cfg["I"], Js, 100.0 * Js / cfg["J"], Js, args.em_iters, args.ref_iters,
+                 float(np.mean(sample_s[args.warmup:])) if args.steps else 0.0))
     line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload(args.config, cfg), "rtol": args.rtol, "em_iters": args.em_iters},
-            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
+            "config": bench_config(args, cfg),
+            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample,
+                             "host": cpu_info(), "extrapolated": True,
+                             "measured_s_per_step": float(np.mean(sample_s[args.warmup:])) if args.steps else 0.0},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def roofline_of(stats, ms_fit, steps, I, J, K, precision):
+    """Roofline of the dominant kernel from the launch accounting of the timed
+    fits.  A tensor-core pass is two launches (operand image, pass), both
+    timed; Hessian passes and gradient-only (EM) passes are counted apart."""
+    peak_hbm, peak_bf16, peak_bf16_sus, peak_src = load_peaks()
+    top = max(("accum_q", "accum_p", "loglik"), key=lambda k: stats[k][1])
+    n_top, ms_top = stats[top]
+    per = 2 if (precision == "mixed" and top in ("accum_q", "accum_p")) else 1
+    launches = max(n_top / per, 1)
+    per_launch_ms = ms_top / launches
+    alg = pass_bytes(top, I, J, K)
+    hbm_gbs = alg / (per_launch_ms * 1e-3) / 1e9
+    share = ms_top / (ms_fit * steps)
+    if top in ("accum_q", "accum_p"):
+        fh, fg = pass_flops(I, J, K)
+        achieved = fh / (per_launch_ms * 1e-3) / 1e12
+        traffic = TRAFFIC_PER_PAIR[top] * I * J if precision == "mixed" else None
+        return {"bound": "tensor", "kernel": top, "achieved": achieved, "peak": peak_bf16_sus,
+                "unit": "TFLOP/s", "frac": achieved / peak_bf16_sus, "traffic": traffic,
+                "traffic_source": "ncu one-pass capture (dram__bytes_read.sum + dram__bytes_write.sum) of one "
+                                  "launch at I=1e5, J=1e5, K=8, per pair x I*J; not measured in this run",
+                "peak_source": peak_src + " (bf16 sustained)", "flops_hessian_per_launch": fh,
+                "flops_gradient_per_launch": fg, "ms_per_launch": per_launch_ms, "launches": int(launches),
+                "secondary_hbm": {"achieved": hbm_gbs, "peak": peak_hbm, "unit": "GB/s",
+                                  "frac": hbm_gbs / peak_hbm, "algorithmic_bytes_per_launch": alg},
+                "share_of_timed": share}
+    return {"bound": "hbm", "kernel": top, "achieved": hbm_gbs, "peak": peak_hbm, "unit": "GB/s",
+            "frac": hbm_gbs / peak_hbm, "traffic": None, "peak_source": peak_src,
+            "algorithmic_bytes_per_launch": alg, "ms_per_launch": per_launch_ms, "launches": int(launches),
+            "share_of_timed": share}
 
 
 def run_ours(args, world, rank, local):
@@ -268,9 +372,8 @@ def run_ours(args, world, rank, local):
         d.set_qp_device(q0_dev.data_ptr(), p0_dev.data_ptr())
         return d.fit(n_iter=args.n_iter, rtol=args.rtol, em_iters=args.em_iters)
 
-    infos = []
     for _ in range(args.warmup):
-        infos.append(step())
+        step()
     d.reset_stats()
     d.set_profiling(True)
     clocks = ClockSampler(local)
@@ -291,91 +394,59 @@ def run_ours(args, world, rank, local):
     launches = int(sum(n for n, _ in stats.values()))
     iters = timed[-1]["iters"]
     ll = timed[-1]["ll"]
-
-    # roofline of the dominant pass kernel.  The accumulation passes are
-    # contractions on the tensor cores: their roofline is the tensor pipe
-    # (achieved = Hessian FLOPs / time against the measured sustained bf16
-    # peak, the kernel running inside a long fit), with the HBM floor as the
-    # secondary bound.  The log-likelihood pass streams the class words (HBM).
-    peak_hbm, peak_bf16, peak_bf16_sus, peak_src = load_peaks()
-    top = max(("accum_q", "accum_p", "loglik"), key=lambda k: stats[k][1])
-    n_top, ms_top = stats[top]
-    # passes of the top kind: in the mixed method a tensor-core pass is two
-    # launches (operand image, pass); the gradient-only EM Q passes run on the
-    # CUDA cores (one launch each)
-    passes = n_top
-    if args.precision == "mixed" and top == "accum_p":
-        passes = n_top / 2
-    elif args.precision == "mixed" and top == "accum_q":
-        em = args.em_iters * args.steps
-        passes = (n_top - em) / 2 + em
-    per_launch_ms = ms_top / max(passes, 1)
-    alg = pass_bytes(top, I, J, K)
-    hbm_gbs = alg / (per_launch_ms * 1e-3) / 1e9
-    if top in ("accum_q", "accum_p"):
-        fh, fg = pass_flops(I, J, K)
-        achieved = fh / (per_launch_ms * 1e-3) / 1e12
-        traffic = TRAFFIC_PER_PAIR[top] * I * J if args.precision == "mixed" else None
-        roofline = {"bound": "tensor", "kernel": top, "achieved": achieved, "peak": peak_bf16_sus,
-                    "unit": "TFLOP/s", "frac": achieved / peak_bf16_sus, "traffic": traffic,
-                    "peak_source": peak_src + " (bf16 sustained)", "flops_hessian_per_launch": fh,
-                    "flops_gradient_per_launch": fg, "ms_per_launch": per_launch_ms,
-                    "secondary_hbm": {"achieved": hbm_gbs, "peak": peak_hbm, "unit": "GB/s",
-                                      "frac": hbm_gbs / peak_hbm, "algorithmic_bytes_per_launch": alg},
-                    "share_of_timed": ms_top / (ms * args.steps)}
-    else:
-        roofline = {"bound": "hbm", "kernel": top, "achieved": hbm_gbs, "peak": peak_hbm, "unit": "GB/s",
-                    "frac": hbm_gbs / peak_hbm, "traffic": None, "peak_source": peak_src,
-                    "algorithmic_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
-                    "share_of_timed": ms_top / (ms * args.steps)}
+    q_c, p_c = d.get_qp()
+    roofline = roofline_of(stats, ms, args.steps, I, J, K, args.precision)
     kernels = {k: {"launches": n, "ms": round(t, 3)} for k, (n, t) in stats.items()}
 
     line = {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
-            "data": "synthetic",
-            "config": {"workload": workload(args.config, cfg),
-                       "method": args.precision, "rtol": args.rtol, "em_iters": args.em_iters,
-                       "outer_iters": iters, "loglik": ll, "parallelism": "replicas" if world > 1 else "1 GPU",
-                       "l2": "inputs (5 GB class words) larger than L2; no flush"},
+            "data": "synthetic", "config": bench_config(args, cfg),
+            "fit": {"method": args.precision, "outer_iters": iters, "loglik": ll,
+                    "parallelism": "replicas" if world > 1 else "1 GPU",
+                    "init_em_loglik": "evaluated after the last of the EM iterations only; the reference "
+                                      "evaluates it after each (src/algorithms_outer.jl:8-12) but only logs "
+                                      "the others, so results are unchanged"},
             "gpu_launches": launches, "kernels": kernels, "roofline": roofline, "clocks": clk}
 
-    # plain FP64 method, per-iteration sample (its full fit takes minutes)
+    # the plain FP64 method from the same start: to convergence (default), or
+    # per-iteration timings only (--plain-estimate)
     if not args.no_plain and rank == 0:
-        dp = hx.GB300Admix(bed_dev.data_ptr(), I, J, K, bytes_per_snp=bps, n_snp=n_snp, precision="fp64",
-                           device=local, bed_on_device=True)
+        dp = hx.GB300Admix.shared(d, K, precision="fp64")
         dp.set_qp_device(q0_dev.data_ptr(), p0_dev.data_ptr())
-        t0 = time.time()
-        dp.init_em(1)
-        t_em = time.time() - t0          # one EM step + its log-likelihood
-        t0 = time.time()
-        dp.loglikelihood()
-        t_ll = time.time() - t0
-        t0 = time.time()
-        dp.qn_iteration()
-        t_it = time.time() - t0
-        # init_em evaluates the log-likelihood after its last step only
-        est = args.em_iters * (t_em - t_ll) + t_ll + iters * t_it
-        line["plain_fp64"] = {"s_per_em_iter": t_em, "s_per_loglik": t_ll, "s_per_outer_iter": t_it,
-                              "est_s_to_converge": est, "est_speedup_chosen_vs_plain": est / (ms / 1e3),
-                              "note": "extrapolated: measured EM and outer-iteration times x the chosen "
-                                      "fit's iteration counts"}
-        if args.plain_full:
-            # the plain fit to convergence from the same start, against the
-            # chosen fit's result (ll relative, Q and P largest absolute)
-            q_c, p_c = d.get_qp()
-            dp.set_qp_device(q0_dev.data_ptr(), p0_dev.data_ptr())
-            torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        if args.plain_estimate:
             t0 = time.time()
+            dp.init_em(1)
+            t_em = time.time() - t0          # one EM step + its log-likelihood
+            t0 = time.time()
+            dp.loglikelihood()
+            t_ll = time.time() - t0
+            t0 = time.time()
+            dp.qn_iteration()
+            t_it = time.time() - t0
+            est = args.em_iters * (t_em - t_ll) + t_ll + iters * t_it
+            line["plain_fp64"] = {"s_per_em_iter": t_em, "s_per_loglik": t_ll, "s_per_outer_iter": t_it,
+                                  "est_s_to_converge": est, "est_speedup_chosen_vs_plain": est / (ms / 1e3),
+                                  "note": "extrapolated: measured EM and outer-iteration times x the chosen "
+                                          "fit's iteration counts"}
+        else:
+            e0.record()
             pinfo = dp.fit(n_iter=args.n_iter, rtol=args.rtol, em_iters=args.em_iters)
-            t_full = time.time() - t0
+            e1.record()
+            torch.cuda.synchronize()
+            t_full = e0.elapsed_time(e1) / 1e3
             q_f, p_f = dp.get_qp()
-            line["plain_fp64"].update({
-                "measured_s_to_converge": t_full, "measured_outer_iters": pinfo["iters"], "ll": pinfo["ll"],
+            rel_ll = abs(ll - pinfo["ll"]) / abs(pinfo["ll"])
+            dq = float(np.abs(q_c - q_f).max())
+            line["plain_fp64"] = {
+                "measured_s_to_converge": t_full, "outer_iters": pinfo["iters"], "loglik": pinfo["ll"],
                 "measured_speedup_chosen_vs_plain": t_full / (ms / 1e3),
-                "chosen_vs_plain": {"ll_rel_diff": abs(ll - pinfo["ll"]) / abs(pinfo["ll"]),
-                                    "q_max_abs_diff": float(np.abs(q_c - q_f).max()),
-                                    "p_max_abs_diff": float(np.abs(p_c - p_f).max())}})
+                "chosen_vs_plain": {"ll_rel_diff": rel_ll, "q_max_abs_diff": dq,
+                                    "p_max_abs_diff": float(np.abs(p_c - p_f).max()),
+                                    "meets_1e-8_ll_and_1e-5_q": bool(rel_ll <= 1e-8 and dq <= 1e-5)},
+                "note": "plain FP64 GPU method fitted to convergence once in this run from the same start "
+                        "(CUDA events); not part of the timed steps"}
         dp.close()
 
     # end to end through the public API from host buffers
@@ -383,7 +454,6 @@ def run_ours(args, world, rank, local):
         host_bed = torch.empty(bps * n_snp, dtype=torch.uint8, pin_memory=True)
         host_bed.copy_(bed_dev)
         hb = host_bed.numpy().reshape(n_snp, bps)
-        q_out = np.empty((K, I), order="F")
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.time()
@@ -400,13 +470,19 @@ def run_ours(args, world, rank, local):
 
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
-        Js = args.cpu_slice_blocks or 200
-        t_em, t_it = cpu_oracle_sample(cfg, Js, threads)
-        v = (args.em_iters * t_em + iters * t_it) * J / Js
-        line["cpu_baseline"] = {"value": v, "unit": "s", "cores": threads, "kind": "port",
-                                "sample": "oracle port, I=%d x %d blocks: 1 EM step + 1 outer iteration, "
-                                          "scaled by J/%d and by this fit's %d EM + %d outer iterations "
-                                          "(extrapolated)" % (I, Js, Js, args.em_iters, iters)}
+        Js = min(args.cpu_slice_blocks or 2000, J)
+        t0 = time.perf_counter()
+        t = cpu_components(cfg, Js, 0, threads, seed=cfg["seed"])
+        spent = time.perf_counter() - t0
+        v, em, outer = cpu_fit_model(t, J, Js, args.em_iters, iters)
+        line["cpu_baseline"] = {
+            "value": v, "unit": "s", "cores": threads, "kind": "port", "host": cpu_info(), "extrapolated": True,
+            "s_per_em_iter": em, "s_per_outer_iter": outer, "measured_s": spent,
+            "pieces_s": {k: round(x, 4) for k, x in t.items()},
+            "sample": "oracle port, %d host threads: J-proportional pieces timed on an I=%d x %d-block slice and "
+                      "scaled by J/%d; I-only pieces (per-individual QPs, projections) and the ZAL point at full "
+                      "size; summed with this fit's %d EM + %d outer iterations (extrapolated)"
+                      % (threads, I, Js, Js, args.em_iters, iters)}
     d.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -48,6 +48,7 @@ struct hx_ctx {
     bool tc = false;                         // Hessian passes on the tensor cores
     int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
     bool have_qp = false;
+    long long wait_budget = HX_WAIT_BUDGET_DEFAULT;   // tensor-core pipeline waits (clock64 cycles)
     std::string err;
     // launch accounting: per kind, kernel launches issued and (when profiling
     // is on) device milliseconds from CUDA events recorded on this stream
@@ -182,6 +183,7 @@ PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
     a.slots = c->slots;
     a.img = c->img;
     a.pf = nullptr;
+    a.budget = c->wait_budget;
     return a;
 }
 
@@ -204,7 +206,7 @@ int pass_q(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
     }
     a.S = c->S_q; a.per_chunk = c->wpc_q; a.part = c->part_q;
     if (c->prec != HX_PREC_FP64) HX_ST(stage_pf(c, p, a));
-    HX_LAUNCH(HX_KIND_ACCUM_Q, 1,
+    HX_LAUNCH(hess ? HX_KIND_ACCUM_Q : HX_KIND_EM_Q, 1,
               c->prec == HX_PREC_FP64 ? launch_accum_q_f64(c->K, hess, a, c->st)
                                       : launch_accum_q_f32(c->K, hess, a, c->st));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_reduce_sym(c->part_q, c->S_q, c->K, hess, c->I, c->Ipad, XtX, Xtz, c->st));
@@ -215,14 +217,14 @@ int pass_p(hx_ctx* c, const double* q, const double* p, bool hess, double* XtX, 
     PassArgs a = pass_args(c, q, p);
     if (c->tc) {
         a.S = c->S_pt; a.per_chunk = c->ipc_pt; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;
-        HX_LAUNCH(HX_KIND_ACCUM_P, 2, launch_accum_p_tc(c->K, hess, a, c->st));
+        HX_LAUNCH(hess ? HX_KIND_ACCUM_P : HX_KIND_EM_P, 2, launch_accum_p_tc(c->K, hess, a, c->st));
         if (c->S_pt > 1)
             HX_LAUNCH(HX_KIND_OTHER, 1,
                       launch_reduce_sym(c->part_p, c->S_pt, c->K, hess, 4 * c->J, 4 * c->J, XtX, Xtz, c->st));
         return HX_OK;
     }
     a.S = c->S_p; a.per_chunk = c->ipc_p; a.part = c->part_p; a.XtX = XtX; a.Xtz = Xtz;
-    HX_LAUNCH(HX_KIND_ACCUM_P, 1,
+    HX_LAUNCH(hess ? HX_KIND_ACCUM_P : HX_KIND_EM_P, 1,
               c->prec == HX_PREC_FP64 ? launch_accum_p_f64(c->K, hess, a, c->st)
                                       : launch_accum_p_f32(c->K, hess, a, c->st));
     if (c->S_p > 1)
@@ -261,6 +263,16 @@ int write_slot(hx_ctx* c, int slot, double v) {
     HX_CK(cudaMemcpyAsync(c->slots + slot, c->h_slots + slot, sizeof(double), cudaMemcpyHostToDevice, c->st));
     HX_CK(cudaStreamSynchronize(c->st));
     return HX_OK;
+}
+
+// After a call's work: HX_ETIMEOUT if a tensor-core pipeline wait ran out
+// since the last check.  The slot is cleared, so the context stays usable (the
+// kernel that timed out drained its copies and MMAs before it exited).
+int take_timeout(hx_ctx* c) {
+    HX_ST(read_slots(c));
+    if (c->h_slots[S_TC_TIMEOUT] == 0.0) return HX_OK;
+    HX_ST(write_slot(c, S_TC_TIMEOUT, 0.0));
+    return fail(c, HX_ETIMEOUT, "tensor-core pass wait timed out");
 }
 
 // em! (src/algorithms_inner.jl:29-84): x -> x_next.  With fix_q / fix_p the
@@ -443,7 +455,7 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     if (Sp_max > 1) HX_ST(dalloc(c, &c->part_p, (size_t)Sp_max * NVmax * 4 * J));
     HX_ST(dalloc(c, &c->part_ll, (size_t)std::max<int64_t>((c->Ipad / ACC_THREADS) * c->S_q,
                                                             (int64_t)loglik_f32x2_blocks(c->Ipad, K) * c->S_ll)));
-    HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (3 * HX_QMAX * HX_QMAX + 2 * HX_QMAX)));
+    HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (2 * HX_QMAX * HX_QMAX + HX_QMAX)));
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));
     if (c->tc) HX_ST(dalloc(c, &c->img, tc_image_bytes(K, I, J)));
@@ -552,7 +564,7 @@ const char* hx_status_string(int s) {
         case HX_EINVAL: return "invalid argument";
         case HX_ECUDA: return "CUDA error";
         case HX_ENAN: return "NaN in gradient or Hessian";
-        case HX_ETIMEOUT: return "iteration cap reached";
+        case HX_ETIMEOUT: return "iteration cap reached, or a device pipeline wait timed out";
         case HX_ENOMEM: return "device out of memory";
         case HX_ESTATE: return "call out of order";
         case HX_EUNSUPPORTED: return "unsupported size";
@@ -679,7 +691,7 @@ int hx_em_accum(hx_ctx* c, const double* q, const double* p, double* q_next, dou
     HX_ST(upload_x(c, q, p, false, c->xio));
     HX_ST(pass_q(c, qof(c->xio), pof(c, c->xio), false, c->XtXq, c->Xtzq));
     HX_ST(pass_p(c, qof(c->xio), pof(c, c->xio), false, c->XtXp, c->Xtzp));
-    HX_CK(cudaStreamSynchronize(c->st));
+    HX_ST(take_timeout(c));
     // numerators q .* Xtz_q and p .* Xtz_p, formed on the host from the copies
     std::vector<double> g((size_t)c->K * std::max<int64_t>(c->I, 4 * c->J));
     if (q_next) {
@@ -702,7 +714,7 @@ int hx_update_q_accum(hx_ctx* c, const double* q, const double* p, double* XtX, 
     if (Xtz) HX_CK(cudaMemcpyAsync(Xtz, c->Xtzq, (size_t)c->K * c->I * sizeof(double), cudaMemcpyDeviceToHost,
                                    c->st));
     HX_CK(cudaStreamSynchronize(c->st));
-    return HX_OK;
+    return take_timeout(c);
 }
 
 int hx_update_p_accum(hx_ctx* c, const double* q, const double* p, double* XtX, double* Xtz) {
@@ -714,6 +726,25 @@ int hx_update_p_accum(hx_ctx* c, const double* q, const double* p, double* XtX, 
     if (Xtz) HX_CK(cudaMemcpyAsync(Xtz, c->Xtzp, (size_t)c->K * 4 * c->J * sizeof(double),
                                    cudaMemcpyDeviceToHost, c->st));
     HX_CK(cudaStreamSynchronize(c->st));
+    return take_timeout(c);
+}
+
+// em_p!(d_cu, g_cu) (src/cuda/runners.jl:51-55; kernels.jl:75-102): the P
+// part of the EM numerators only, p_next[k,m] = p[k,m] Xtz_p[k,m].
+int hx_em_p_accum(hx_ctx* c, const double* q, const double* p, double* p_next) {
+    if (!c || !q || !p || !p_next) return HX_EINVAL;
+    HX_ST(upload_x(c, q, p, false, c->xio));
+    HX_ST(pass_p(c, qof(c->xio), pof(c, c->xio), false, c->XtXp, c->Xtzp));
+    HX_ST(take_timeout(c));
+    std::vector<double> g((size_t)c->K * 4 * c->J);
+    HX_CK(cudaMemcpy(g.data(), c->Xtzp, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t a = 0; a < g.size(); ++a) p_next[a] = p[a] * g[a];
+    return HX_OK;
+}
+
+int hx_set_wait_budget(hx_ctx* c, int64_t cycles) {
+    if (!c) return HX_EINVAL;
+    c->wait_budget = cycles > 0 ? (long long)cycles : (long long)HX_WAIT_BUDGET_DEFAULT;
     return HX_OK;
 }
 
@@ -794,7 +825,7 @@ int hx_zal(hx_ctx* c, const double* x, const double* x_next, const double* x_nex
     double* dU = t.get<double>(c, (size_t)n * Qs, &st);
     double* dV = t.get<double>(c, (size_t)n * Qs, &st);
     double* dxt = t.get<double>(c, n, &st);
-    double* part = t.get<double>(c, (size_t)qn_dots_blocks(n) * (3 * HX_QMAX * HX_QMAX + 2 * HX_QMAX), &st);
+    double* part = t.get<double>(c, (size_t)qn_dots_blocks(n) * (2 * HX_QMAX * HX_QMAX + HX_QMAX), &st);
     double* coef = t.get<double>(c, HX_QMAX, &st);
     double* slots = t.get<double>(c, HX_NSLOT, &st);
     if (st != HX_OK) return st;
@@ -817,8 +848,7 @@ int hx_zal(hx_ctx* c, const double* x, const double* x_next, const double* x_nex
 int hx_em_step(hx_ctx* c) {
     HX_ST(check_qp(c));
     HX_ST(em_step(c));
-    HX_CK(cudaStreamSynchronize(c->st));
-    return HX_OK;
+    return take_timeout(c);
 }
 
 // init_em! (src/algorithms_outer.jl:1-22).  The log-likelihood of every EM
@@ -837,14 +867,13 @@ int hx_init_em(hx_ctx* c, int32_t iters) {
             fprintf(stderr, "{\"em_iter\": %d, \"ll\": %.17g}\n", e + 1, c->h_slots[S_LL_NEW]);
         }
     }
-    HX_CK(cudaStreamSynchronize(c->st));
-    return HX_OK;
+    return take_timeout(c);
 }
 
 int hx_update_q(hx_ctx* c, int32_t update2) {
     HX_ST(check_qp(c));
     HX_ST(update_q(c, update2 != 0));
-    HX_ST(read_slots(c));
+    HX_ST(take_timeout(c));     // a pass that timed out leaves garbage sums: report the cause first
     if (c->h_slots[S_NAN] != 0.0) return fail(c, HX_ENAN, "NaN in XtX_q/Xtz_q");
     return HX_OK;
 }
@@ -852,8 +881,7 @@ int hx_update_q(hx_ctx* c, int32_t update2) {
 int hx_update_p(hx_ctx* c, int32_t update2) {
     HX_ST(check_qp(c));
     HX_ST(update_p(c, update2 != 0));
-    HX_CK(cudaStreamSynchronize(c->st));
-    return HX_OK;
+    return take_timeout(c);
 }
 
 int hx_qn_iteration(hx_ctx* c, hx_iter_info* info) {
@@ -882,8 +910,8 @@ int hx_qn_iteration(hx_ctx* c, hx_iter_info* info) {
                 "{\"iter\": %d, \"ll\": %.17g, \"reldiff\": %.6e, \"ll_basic\": %.17g, \"ll_qn\": %.17g, "
                 "\"qn\": %d, \"ms\": %.3f}\n",
                 (int)s[S_ITER], s[S_LL_NEW], s[S_RELDIFF], s[S_LL_BASIC], s[S_LL_QN], (int)s[S_ACCEPT_QN], ms);
+    HX_ST(take_timeout(c));
     if (s[S_NAN] != 0.0) return fail(c, HX_ENAN, "NaN in XtX_q/Xtz_q");
-    if (s[S_TC_TIMEOUT] != 0.0) return fail(c, HX_ETIMEOUT, "tensor-core pass wait timed out");
     return HX_OK;
 }
 

@@ -18,13 +18,9 @@ namespace hx {
 namespace {
 
 constexpr int NA_THREADS = 128;
-constexpr int NA_MAX_DEVICES = 64;
 
 // Scratch of the no-allocation entry point: one FP64 partial per CTA.
 __device__ __align__(256) double g_noalloc_scratch[HX_NOALLOC_SCRATCH];
-
-// Device address of g_noalloc_scratch per device ordinal, resolved once.
-double* g_scratch_ptr[NA_MAX_DEVICES] = {nullptr};
 
 // One individual per thread over a chunk of blocks, decoding the two SNP codes
 // of each block straight from the BED bytes (src/loops.jl:55-71); pair
@@ -65,6 +61,27 @@ k_loglik_bed(const uint8_t* __restrict__ bed, int64_t bps, int64_t I, int64_t J,
             }
             T L, u[4];
             pair_eval<T>(nib, qp, L, u);
+            if (sizeof(T) == 4 && L < T(1.17549435e-38f) && L == L) {
+                // FP32 pair likelihood below the smallest normal float (caller
+                // Q/P entries far below the fit's 1e-5 floor): the renormaliser
+                // reads the exponent field, so redo this pair in FP64 and fold
+                // its mantissa and exponent in separately
+                double qd[4], Ld, ud[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    double s = 0.0;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) s = fma((double)q[(int64_t)K * i + k], pj[h * K + k], s);
+                    qd[h] = s;
+                }
+                pair_eval<double>(nib, qd, Ld, ud);
+                if (!(Ld > 0.0)) {
+                    if (Ld == 0.0) zero = true; else bad = true;
+                    continue;
+                }
+                mant = renorm(mant * (T)renorm(Ld, ex), ex);
+                continue;
+            }
             if (!(L > T(0))) {
                 if (L == T(0)) zero = true; else bad = true;
                 L = T(1);
@@ -126,16 +143,15 @@ extern "C" int hx_loglikelihood_noalloc(const uint8_t* d_bed, int64_t bytes_per_
     // one partial per CTA: (individual tiles) x (block chunks) must fit the static scratch
     const int64_t tiles = (I + NA_THREADS - 1) / NA_THREADS;
     if (tiles > HX_NOALLOC_SCRATCH) return HX_EUNSUPPORTED;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return HX_ECUDA;
-    // set-up, once per device with that device current: the device address of
-    // the scratch array (host code may not use the symbol itself as an address)
-    if (!g_scratch_ptr[dev]) {
-        void* ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return HX_ECUDA;
-        g_scratch_ptr[dev] = (double*)ptr;
-    }
-    double* scratch = g_scratch_ptr[dev];
+    // The device address of the scratch array in the current device's
+    // context (host code may not use the symbol itself as an address).  It is
+    // looked up on every call, not cached: after a device or primary-context
+    // reset the module is loaded again at another address.  The lookup
+    // allocates nothing; the first call in a context also loads the module,
+    // so make that first call before any stream capture.
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return HX_ECUDA;
+    double* scratch = (double*)ptr;
     const int64_t target = 2048;
     int64_t S = std::max<int64_t>(1, std::min<int64_t>(J, (target + tiles - 1) / tiles));
     S = std::min<int64_t>(S, HX_NOALLOC_SCRATCH / tiles);

@@ -624,13 +624,14 @@ k_qp_p(int K, int64_t n, const double* __restrict__ XtX, const double* __restric
 // ------------------------------------------------------------------ ZAL QN
 constexpr int QN_THREADS = 256;
 
-// Secant-pair update and the dot products of the QN point: UtU (full), UtV,
-// Utd with d = x - x_next, and for LB (the LBQN step) also VtV and Vtd.
+// Secant-pair update and the dot products of the QN point: for ZAL UtU (full),
+// UtV and Utd with d = x - x_next; for LB (the LBQN step) YtY and Ytd with
+// Y = U - V formed per element (a short Y, v close to u, keeps its accuracy).
 template <int QS, bool LB>
 __global__ void __launch_bounds__(QN_THREADS)
 k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn, const double* __restrict__ xn2,
           double* __restrict__ U, double* __restrict__ V, const double* __restrict__ slots, double* __restrict__ part) {
-    constexpr int NV = QS * QS * 2 + QS + (LB ? QS * QS + QS : 0);
+    constexpr int NV = LB ? QS * QS + QS : QS * QS * 2 + QS;
     __shared__ double red[QN_THREADS / 32][NV];
     const int it = (int)slots[S_ITER];
     const int col = (it > 0 ? it - 1 : 0) % QS;
@@ -649,16 +650,26 @@ k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn
             v[r] = (r == col) ? va : V[a + n * r];
         }
         const double dxa = xa - xna;
+        if (LB) {
+            double y[QS];
 #pragma unroll
-        for (int r = 0; r < QS; ++r) {
+            for (int r = 0; r < QS; ++r) y[r] = u[r] - v[r];
 #pragma unroll
-            for (int s = 0; s < QS; ++s) {
-                acc[r * QS + s] += u[r] * u[s];
-                acc[QS * QS + r * QS + s] += u[r] * v[s];
-                if (LB) acc[2 * QS * QS + QS + r * QS + s] += v[r] * v[s];
+            for (int r = 0; r < QS; ++r) {
+#pragma unroll
+                for (int s = 0; s < QS; ++s) acc[r * QS + s] += y[r] * y[s];
+                acc[QS * QS + r] += y[r] * dxa;
             }
-            acc[2 * QS * QS + r] += u[r] * dxa;
-            if (LB) acc[3 * QS * QS + QS + r] += v[r] * dxa;
+        } else {
+#pragma unroll
+            for (int r = 0; r < QS; ++r) {
+#pragma unroll
+                for (int s = 0; s < QS; ++s) {
+                    acc[r * QS + s] += u[r] * u[s];
+                    acc[QS * QS + r * QS + s] += u[r] * v[s];
+                }
+                acc[2 * QS * QS + r] += u[r] * dxa;
+            }
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -684,8 +695,8 @@ k_qn_dots(int64_t n, const double* __restrict__ x, const double* __restrict__ xn
 // LBQN (lb = 1) (U-V)'(U-V) c = (U-V)'d.
 __global__ void k_qn_solve(const double* __restrict__ part, int nblk, int QS, const double* __restrict__ slots,
                            double* __restrict__ coef, int lb) {
-    __shared__ double tot[3 * HX_QMAX_DEV * HX_QMAX_DEV + 2 * HX_QMAX_DEV];
-    const int NV = QS * QS * 2 + QS + (lb ? QS * QS + QS : 0);
+    __shared__ double tot[2 * HX_QMAX_DEV * HX_QMAX_DEV + HX_QMAX_DEV];
+    const int NV = lb ? QS * QS + QS : QS * QS * 2 + QS;
     for (int v = threadIdx.x; v < NV; v += blockDim.x) {
         double s = 0.0;
         for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * NV + v];
@@ -696,14 +707,10 @@ __global__ void k_qn_solve(const double* __restrict__ part, int nblk, int QS, co
     const int it = (int)slots[S_ITER];
     const int m = it < QS ? it : QS;
     double A[HX_QMAX_DEV * HX_QMAX_DEV], b[HX_QMAX_DEV];
-    const double* VtV = tot + 2 * QS * QS + QS;
-    const double* Vtd = tot + 3 * QS * QS + QS;
     for (int r = 0; r < m; ++r) {
-        for (int s = 0; s < m; ++s) {
-            const double uu = tot[r * QS + s], uv = tot[QS * QS + r * QS + s];
-            A[r + m * s] = lb ? ((uu - uv) - tot[QS * QS + s * QS + r]) + VtV[r * QS + s] : uu - uv;
-        }
-        b[r] = lb ? tot[2 * QS * QS + r] - Vtd[r] : tot[2 * QS * QS + r];
+        for (int s = 0; s < m; ++s)
+            A[r + m * s] = lb ? tot[r * QS + s] : tot[r * QS + s] - tot[QS * QS + r * QS + s];
+        b[r] = lb ? tot[QS * QS + r] : tot[2 * QS * QS + r];
     }
     for (int c = 0; c < m; ++c) {
         int piv = c;

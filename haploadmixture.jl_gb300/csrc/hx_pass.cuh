@@ -49,6 +49,7 @@ struct PassArgs {
     uint8_t* img;           // tensor-core passes: B-operand image of the pass (written by the pass)
     const float* pf;        // FP32 copy of p for the FP32 passes that stage p (or null): GB300's
                             // FP64 unit is narrow, and converting in every CTA kept it busy
+    long long budget;       // tensor-core passes: clock64 cycles any one pipeline wait may take
 };
 
 template <int K> __device__ __forceinline__ constexpr int tri(int k, int k2) {

@@ -35,7 +35,8 @@
 // stage s-2 with stage s-2+RING; every warp generates its part of the A tiles and arrives on
 // a shared counter; the last arriving warp issues the stage's MMAs and commits
 // them to an mbarrier.  Warps therefore run up to two stages apart, and two CTAs (16 warps)
-// share an SM.  Every wait is bounded (TC_BUDGET cycles); a timeout sets
+// share an SM.  Every wait is bounded (PassArgs::budget cycles, by default
+// TC_BUDGET; the drain after a timeout always allows TC_BUDGET); a timeout sets
 // slots[S_TC_TIMEOUT] and the CTA drains and exits.
 #pragma once
 #include <algorithm>
@@ -511,8 +512,8 @@ __device__ __forceinline__ void arrive_generated(Sync* sy, int b) {
     if ((threadIdx.x & 31) == 0) mbar_arrive(&sy->gen_full[b]);
 }
 // An issuer (lane 0 of a fixed warp) waits until the whole stage is generated.
-__device__ __forceinline__ bool wait_generated(Sync* sy, int s, int b, double* slots) {
-    if (!mbar_wait(&sy->gen_full[b], (s >> 1) & 1, TC_BUDGET)) { set_bad(sy, slots); return false; }
+__device__ __forceinline__ bool wait_generated(Sync* sy, int s, int b, double* slots, long long budget) {
+    if (!mbar_wait(&sy->gen_full[b], (s >> 1) & 1, budget)) { set_bad(sy, slots); return false; }
     fence_after();
     return true;
 }
@@ -523,13 +524,13 @@ __device__ __forceinline__ bool wait_generated(Sync* sy, int s, int b, double* s
 // once every thread has arrived there).
 constexpr int FOLD_OFF = TC_FLUSH / 2;
 template <int K, bool STACK>
-__device__ __forceinline__ void maybe_fold(Sync* sy, double* slots, int hf, int s, uint32_t taddr_lane, float* acc,
+__device__ __forceinline__ void maybe_fold(Sync* sy, double* slots, long long budget, int hf, int s, uint32_t taddr_lane, float* acc,
                                            float* comp) {
     using D = TcDims<K>;
     constexpr int WC = STACK ? D::WS : D::WQ;   // TMEM columns per window
     if (s >= TC_FLUSH + FOLD_OFF && (s - FOLD_OFF) % TC_FLUSH == 0) {
         const int wp = (s - FOLD_OFF) / TC_FLUSH - 1;
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, TC_BUDGET));
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[wp & 1], (wp >> 1) & 1, budget));
         if (!ok) set_bad(sy, slots);
         else {
             fence_after();
@@ -540,7 +541,7 @@ __device__ __forceinline__ void maybe_fold(Sync* sy, double* slots, int hf, int 
 }
 
 template <int K, bool STACK>
-__device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int ns, uint32_t taddr_lane, float* acc,
+__device__ __forceinline__ void final_fold(Sync* sy, double* slots, long long budget, int hf, int ns, uint32_t taddr_lane, float* acc,
                                            float* comp) {
     using D = TcDims<K>;
     constexpr int WC = STACK ? D::WS : D::WQ;
@@ -550,7 +551,7 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, int hf, int 
         const int wl = (ns - 1) / TC_FLUSH;
         const int nf = ns - 1 >= FOLD_OFF ? (ns - 1 - FOLD_OFF) / TC_FLUSH : 0;
         for (int w = nf; w <= wl; ++w) {
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[w & 1], (w >> 1) & 1, TC_BUDGET));
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->flush_done[w & 1], (w >> 1) & 1, budget));
             if (!ok) { set_bad(sy, slots); break; }
             fence_after();
             fold_half<K, STACK>(hf, taddr_lane, (w & 1) * WC, acc, comp);
@@ -599,6 +600,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     uint32_t* SW = (uint32_t*)(smem + (sRq - sA) + QRING * GBQ);     // [RING][128]
     Sync* sy = (Sync*)(SW + RING * 128);
     __shared__ float4 s_snp[4];
+    const long long budget = a.budget;
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int r = tid & 127, hf = tid >> 7;
@@ -669,7 +671,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
     // qp of stages 0 and 1; stage t's qp is then issued at stage t-2
     if (tid == 0) {
         for (int t = 0; t < 2 && t < ns; ++t) {
-            if (!mbar_wait(&sy->fullq[t], 0, TC_BUDGET)) { set_bad(sy, a.slots); break; }
+            if (!mbar_wait(&sy->fullq[t], 0, budget)) { set_bad(sy, a.slots); break; }
             fence_after();
             issue_qp<K>(tq + t * 32, sAq, sRq + t * GBQ);
             commit(&sy->qp_done[t]);
@@ -678,10 +680,10 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
 
     for (int s = 0; s < ns; ++s) {
         const int b = s & 1, slot = s % RING;
-        if (!mbar_wait(&sy->full[slot], (s / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        if (!mbar_wait(&sy->full[slot], (s / RING) & 1, budget)) set_bad(sy, a.slots);
         // A buffer b was last read by the MMAs of stage s-2
         if (s >= 2 && !is_bad(sy))
-            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, budget)) set_bad(sy, a.slots);
         if (is_bad(sy)) break;
         // ring refill: the slot of stage s-2 is free (its MMAs are done -- just
         // waited for -- and they were issued after every thread had read it).
@@ -700,7 +702,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         float qpv[16];
         {
             if (s < 2) {
-                const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], 0, TC_BUDGET));
+                const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], 0, budget));
                 if (!ok) { set_bad(sy, a.slots); break; }
             }
             fence_after();
@@ -736,12 +738,12 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
         // s+2 into this stage's qp columns (every thread has read them).  Each
         // commits to mma_done, which therefore also covers the qp MMA.
         if ((tid & 31) == 0 && (warp == 2 || warp == 4 || (HESS && warp == 0))) {
-            if (wait_generated(sy, s, b, a.slots)) {
+            if (wait_generated(sy, s, b, a.slots, budget)) {
                 const int d = (s / TC_FLUSH) & 1;
                 if (warp == 4) {
                     if (s + 2 < ns) {
                         const int qs = (s + 2) % QRING;
-                        if (!mbar_wait(&sy->fullq[qs], ((s + 2) / QRING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+                        if (!mbar_wait(&sy->fullq[qs], ((s + 2) / QRING) & 1, budget)) set_bad(sy, a.slots);
                         else issue_qp<K>(tq + b * 32, sAq, sRq + qs * GBQ);
                     }
                     commit_stage(sy, s, ns, b, false);
@@ -759,9 +761,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
                 }
             }
         }
-        maybe_fold<K, false>(sy, a.slots, hf, s, taddr_lane, acc, comp);
+        maybe_fold<K, false>(sy, a.slots, budget, hf, s, taddr_lane, acc, comp);
     }
-    final_fold<K, false>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
+    final_fold<K, false>(sy, a.slots, budget, hf, ns, taddr_lane, acc, comp);
     // write partials: v < K gradient, v = K + tri index Hessian
     constexpr int NV = K + (HESS ? D::NH : 0);
     double* out = a.part + (int64_t)blockIdx.y * NV * a.Ipad;
@@ -824,6 +826,7 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
     uint32_t* SW = (uint32_t*)(smem + (sR - sA) + RING * GB);        // [RING][4][KD]
     Sync* sy = (Sync*)(SW + RING * 4 * KD);
     __shared__ float4 s_snp[4];
+    const long long budget = a.budget;
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int jl = tid >> 3, ig = tid & 7;
@@ -884,9 +887,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
 
     for (int s = 0; s < ns; ++s) {
         const int b = s & 1, slot = s % RING;
-        if (!mbar_wait(&sy->full[slot], (s / RING) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+        if (!mbar_wait(&sy->full[slot], (s / RING) & 1, budget)) set_bad(sy, a.slots);
         if (s >= 2 && !is_bad(sy))
-            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, TC_BUDGET)) set_bad(sy, a.slots);
+            if (!mbar_wait(&sy->mma_done[b], ((s - 2) >> 1) & 1, budget)) set_bad(sy, a.slots);
         if (is_bad(sy)) break;
         // ring refill by the first warp here (see the Q side)
         if (s >= 2 && s - 2 + RING < ns && first_at_stage(&sy->started[b])) load_stage(s - 2 + RING);
@@ -941,9 +944,9 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_p_tc(Pass
                                          (s % TC_FLUSH) == 0);
             commit_stage(sy, s, ns, b);
         }
-        maybe_fold<K, true>(sy, a.slots, hf, s, taddr_lane, acc, comp);
+        maybe_fold<K, true>(sy, a.slots, budget, hf, s, taddr_lane, acc, comp);
     }
-    final_fold<K, true>(sy, a.slots, hf, ns, taddr_lane, acc, comp);
+    final_fold<K, true>(sy, a.slots, budget, hf, ns, taddr_lane, acc, comp);
     // rows m of this CTA: TMEM lane r
     const int r = tid & 127;
     const int64_t m = (int64_t)blockIdx.x * 128 + r;

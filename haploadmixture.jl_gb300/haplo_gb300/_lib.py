@@ -75,6 +75,8 @@ SIGNATURES = {
     "hx_em_accum": (I32, [P, P, P, P, P]),
     "hx_update_q_accum": (I32, [P, P, P, P, P]),
     "hx_update_p_accum": (I32, [P, P, P, P, P]),
+    "hx_em_p_accum": (I32, [P, P, P, P]),
+    "hx_set_wait_budget": (I32, [P, I64]),
     "hx_qp_q": (I32, [P, I64, P, P, P, P]),
     "hx_qp_p": (I32, [P, I64, P, P, P, P]),
     "hx_project_q": (I32, [P, I64, P]),

@@ -170,7 +170,7 @@ class GB300Admix:
         return d
 
     # -- launch accounting
-    KINDS = ("accum_q", "accum_p", "loglik", "qp_q", "qp_p", "qn", "other")
+    KINDS = ("accum_q", "accum_p", "loglik", "qp_q", "qp_p", "qn", "other", "em_q", "em_p")
 
     def set_loop_opts(self, fix_q=False, fix_p=False, guarantee_increase=False, penalty=None, mode="ZAL"):
         """admixture_qn!/init_em! keyword options (src/algorithms_outer.jl:1-3, 38-41);
@@ -215,6 +215,19 @@ class GB300Admix:
         pn = np.empty_like(pa, order="F")
         self._ck(self.lib.hx_em_accum(self._h, ptr(qa), ptr(pa), ptr(qn), ptr(pn)))
         return qn, pn
+
+    def em_p_accum(self, q, p):
+        """em_p! (src/cuda/runners.jl:51-55): the P numerators p .* Xtz_p only."""
+        qa, pa = _fortran(q, (self.K, self.I)), _fortran(p, (self.K, 4 * self.J))
+        pn = np.empty_like(pa, order="F")
+        self._ck(self.lib.hx_em_p_accum(self._h, ptr(qa), ptr(pa), ptr(pn)))
+        return pn
+
+    def set_wait_budget(self, cycles=0):
+        """Bound (SM clock cycles) on each pipeline wait of the tensor-core
+        passes; 0 restores the default.  A wait that runs out raises HxError
+        with status HX_ETIMEOUT and leaves the handle usable."""
+        self._ck(self.lib.hx_set_wait_budget(self._h, int(cycles)))
 
     def update_q_accum(self, q, p):
         qa, pa = _fortran(q, (self.K, self.I)), _fortran(p, (self.K, 4 * self.J))

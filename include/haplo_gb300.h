@@ -34,7 +34,8 @@ extern "C" {
 #define HX_EINVAL 1        /* bad argument or size */
 #define HX_ECUDA 2         /* CUDA runtime error, or no device */
 #define HX_ENAN 3          /* NaN in a gradient/Hessian (src/algorithms_inner.jl:132-133) */
-#define HX_ETIMEOUT 4      /* an iteration cap was hit */
+#define HX_ETIMEOUT 4      /* an iteration cap was hit, or a tensor-core pipeline wait ran out
+                              (hx_set_wait_budget); the context stays usable */
 #define HX_ENOMEM 5        /* device allocation failed */
 #define HX_ESTATE 6        /* call out of order (e.g. no Q/P set yet) */
 #define HX_EUNSUPPORTED 7  /* K outside 1..HX_KMAX, or secant count outside 1..HX_QMAX */
@@ -138,6 +139,17 @@ int hx_em_accum(hx_ctx* ctx, const double* q, const double* p, double* q_next, d
 int hx_update_q_accum(hx_ctx* ctx, const double* q, const double* p, double* XtX, double* Xtz);
 /* update_p_cuda!(d_cu, g_cu) (runners.jl:89-92; kernels.jl:140-175). */
 int hx_update_p_accum(hx_ctx* ctx, const double* q, const double* p, double* XtX, double* Xtz);
+/* em_p!(d_cu, g_cu) raw P numerators only (runners.jl:51-55; kernels.jl:75-102). */
+int hx_em_p_accum(hx_ctx* ctx, const double* q, const double* p, double* p_next);
+
+/* Bound on any one pipeline wait of the tensor-core passes, in SM clock
+ * cycles (clock64).  No reference counterpart (CUDA.jl kernels never wait on
+ * one another).  A wait that runs out makes the pass stop early: it drains the
+ * copies and MMAs it issued (each such wait allowed HX_WAIT_BUDGET_DEFAULT
+ * cycles), releases its tensor memory, and the call returns HX_ETIMEOUT with
+ * the context still usable.  cycles <= 0 restores the default. */
+#define HX_WAIT_BUDGET_DEFAULT 4000000000LL
+int hx_set_wait_budget(hx_ctx* ctx, int64_t cycles);
 
 /* ---- batched QP / projection (CPU-only in the reference) on host arrays ---- */
 /* Per individual: argmin 0.5 d'Hd - g'd, sum d = 0, 0 <= q+d <= 1 with
@@ -225,14 +237,16 @@ int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int
 
 /* ---- launch accounting (no counterpart in the reference, which prints
  * @time per phase, src/algorithms_inner.jl:114,135,241,259) ---- */
-#define HX_KIND_ACCUM_Q 0  /* Q-side gradient/Hessian pass */
-#define HX_KIND_ACCUM_P 1  /* P-side gradient/Hessian pass */
+#define HX_KIND_ACCUM_Q 0  /* Q-side gradient+Hessian pass */
+#define HX_KIND_ACCUM_P 1  /* P-side gradient+Hessian pass */
 #define HX_KIND_LOGLIK 2   /* log-likelihood pass */
 #define HX_KIND_QP_Q 3     /* batched per-individual QP */
 #define HX_KIND_QP_P 4     /* batched per-block QP */
 #define HX_KIND_QN 5       /* ZAL secant update, solve and step */
 #define HX_KIND_OTHER 6    /* reductions, projections, bookkeeping */
-#define HX_NKIND 7
+#define HX_KIND_EM_Q 7     /* Q-side gradient-only pass (EM numerators) */
+#define HX_KIND_EM_P 8     /* P-side gradient-only pass (EM numerators) */
+#define HX_NKIND 9
 /* on != 0: record CUDA events around every launch on the context's stream. */
 int hx_set_profiling(hx_ctx* ctx, int32_t on);
 /* Launches issued (always counted) and device ms (while profiling) of a kind. */
@@ -265,9 +279,13 @@ int hx_synth_bed_device(uint64_t seed, int64_t I, int64_t J, int32_t K, const ui
  *
  * Its only scratch is a file-scope device array of HX_NOALLOC_SCRATCH doubles
  * (256 KB), held by every GPU that loads this library until the process exits.
- * The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress, with the device current); make that first call before
- * any stream capture.  Every call shares the array and leaves its partial sums
+ * Every call looks up that array's device address in the current device's
+ * context (cudaGetSymbolAddress, which allocates nothing), so a device reset
+ * between calls is safe; the first call in a context also loads the module,
+ * so make that first call before any stream capture.  Q and P may hold any
+ * values in [0, 1]; in the mixed method a pair whose FP32 likelihood falls
+ * below the smallest normal float is evaluated in FP64.  Every call shares the
+ * array and leaves its partial sums
  * in it; each call overwrites all the partials it reads, so nothing needs to
  * start at zero.  Calls that overlap on the GPU (different streams, or other
  * host threads) race on the array and must be serialised by the caller.

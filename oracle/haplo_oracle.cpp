@@ -787,23 +787,24 @@ void qn_point(int64_t n, const double* x, const double* x_next, const double* x_
     }
     int m = it < Qs ? it : Qs;
     std::vector<double> A(m * m), b(m);
+    // ZAL: (U'U - U'V) c = U'd.  LBQN: Y'Y c = Y'd with Y = U - V formed per
+    // element, so that a short Y (v close to u, slow EM) keeps its accuracy.
     for (int r = 0; r < m; ++r) {
         for (int s = 0; s < m; ++s) {
-            double uu = 0.0, uv = 0.0, vu = 0.0, vv = 0.0;
+            double uu = 0.0, uv = 0.0, yy = 0.0;
             for (int64_t a = 0; a < n; ++a) {
                 uu += U[a + n * r] * U[a + n * s];
                 uv += U[a + n * r] * V[a + n * s];
-                vu += V[a + n * r] * U[a + n * s];
-                vv += V[a + n * r] * V[a + n * s];
+                yy += (U[a + n * r] - V[a + n * r]) * (U[a + n * s] - V[a + n * s]);
             }
-            A[r + m * s] = mode == 1 ? ((uu - uv) - vu) + vv : uu - uv;
+            A[r + m * s] = mode == 1 ? yy : uu - uv;
         }
-        double t = 0.0, tv = 0.0;
+        double t = 0.0, ty = 0.0;
         for (int64_t a = 0; a < n; ++a) {
             t += U[a + n * r] * (x[a] - x_next[a]);
-            tv += V[a + n * r] * (x[a] - x_next[a]);
+            ty += (U[a + n * r] - V[a + n * r]) * (x[a] - x_next[a]);
         }
-        b[r] = mode == 1 ? t - tv : t;
+        b[r] = mode == 1 ? ty : t;
     }
     solve_small(m, A, b);
     for (int64_t a = 0; a < n; ++a) {

@@ -73,6 +73,7 @@ def test_loglik_and_accumulations_fp64_all_K(hx, O, K):
     qn, pn = d.em_accum(q, p)
     oq, op = O.em_accum(b, K, q, p)
     assert rel_err(qn, oq) < 1e-12 and rel_err(pn, op) < 1e-12
+    assert rel_err(d.em_p_accum(q, p), op) < 1e-12      # em_p! runner
 
 
 def test_loglik_formulas_and_injected_state(hx, O, coh):

@@ -29,20 +29,34 @@ def _reference_ll(hx, c, q, p, precision):
         d.close()
 
 
-def _noalloc_ll(hx, c, q, p, precision):
+def _device_inputs(c, q, p):
     import torch
-    from haplo_gb300 import _lib
-    lib = hx.load()
     dev = torch.device("cuda", 0)
     bed = torch.from_numpy(np.ascontiguousarray(c["bed"])).to(dev)
     dq = torch.from_numpy(np.ascontiguousarray(np.asfortranarray(q).T)).to(dev)      # column-major K x I
     dp = torch.from_numpy(np.ascontiguousarray(np.asfortranarray(p).T)).to(dev)
     out = torch.full((1,), float("nan"), dtype=torch.float64, device=dev)
+    return bed, dq, dp, out
+
+
+def _call(lib, c, bed, dq, dp, out, prec, stream):
+    return lib.hx_loglikelihood_noalloc(C.c_void_p(bed.data_ptr()), c["bed"].shape[1], c["I"], c["J"], c["K"],
+                                        C.c_void_p(dq.data_ptr()), C.c_void_p(dp.data_ptr()), prec,
+                                        C.c_void_p(out.data_ptr()), stream)
+
+
+def _noalloc_ll(hx, c, q, p, precision, stream=None):
+    import torch
+    from haplo_gb300 import _lib
+    lib = hx.load()
+    bed, dq, dp, out = _device_inputs(c, q, p)
     prec = {"fp64": _lib.HX_PREC_FP64, "mixed": _lib.HX_PREC_MIXED}[precision]
-    st = lib.hx_loglikelihood_noalloc(C.c_void_p(bed.data_ptr()), c["bed"].shape[1], c["I"], c["J"], c["K"],
-                                      C.c_void_p(dq.data_ptr()), C.c_void_p(dp.data_ptr()), prec,
-                                      C.c_void_p(out.data_ptr()), None)
+    torch.cuda.synchronize()
+    handle = None if stream is None else C.c_void_p(stream.cuda_stream)
+    st = _call(lib, c, bed, dq, dp, out, prec, handle)
     assert st == _lib.HX_OK, lib.hx_status_string(st)
+    if stream is not None:
+        stream.synchronize()
     torch.cuda.synchronize()
     return float(out.item())
 
@@ -57,6 +71,48 @@ def test_noalloc_matches_context_entry_point_two_calls(hx, precision, rel):
         want = _reference_ll(hx, c, q, p, precision)
         got = _noalloc_ll(hx, c, q, p, precision)
         assert got == pytest.approx(want, rel=rel)
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64", 1e-12), ("mixed", 1e-9)])
+def test_noalloc_on_caller_stream(hx, precision, rel):
+    """The kernels are enqueued on the caller's stream (a torch stream here),
+    and a call leaves the free device memory unchanged."""
+    import torch
+    from haplo_gb300 import _lib
+    from haplo_gb300.admix import random_init
+    c = small_cohort(515, 203, 5, seed=33, miss=0.02)
+    q, p = random_init(c["I"], c["J"], c["K"], np.random.default_rng(3))
+    want = _reference_ll(hx, c, q, p, precision)
+    s = torch.cuda.Stream()
+    assert _noalloc_ll(hx, c, q, p, precision, stream=s) == pytest.approx(want, rel=rel)
+    # after a first call (module loaded), further calls allocate nothing
+    lib = hx.load()
+    bed, dq, dp, out = _device_inputs(c, q, p)
+    prec = {"fp64": _lib.HX_PREC_FP64, "mixed": _lib.HX_PREC_MIXED}[precision]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert _call(lib, c, bed, dq, dp, out, prec, C.c_void_p(s.cuda_stream)) == _lib.HX_OK
+    s.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert float(out.item()) == pytest.approx(want, rel=rel)
+
+
+def test_noalloc_mixed_tiny_pair_likelihoods(hx):
+    """Q/P entries far below the fit's 1e-5 floor give FP32 pair likelihoods
+    below the smallest normal float; the mixed method still matches FP64."""
+    from haplo_gb300.admix import random_init
+    c = small_cohort(260, 40, 3, seed=34, miss=0.02)
+    q, p = random_init(c["I"], c["J"], c["K"], np.random.default_rng(4))
+    p = p.copy()
+    # block 0: haplotype 00 nearly impossible in every population
+    p[:, 0] = 1e-22
+    p[:, 1:4] /= p[:, 1:4].sum(axis=1, keepdims=True) / (1 - 1e-22)
+    want = _reference_ll(hx, c, q, p, "fp64")
+    got = _noalloc_ll(hx, c, q, p, "mixed")
+    assert np.isfinite(got)
+    assert got == pytest.approx(want, rel=1e-7)
 
 
 def test_noalloc_rejects_sizes_beyond_scratch(hx):
