@@ -1049,7 +1049,7 @@ int hx_lws_train(const float* d_feat, const float* d_target, int64_t n, int32_t 
     return cuda_status(e);
 }
 
-int hx_lws_warm_start(hx_ctx* c, const float* params, int32_t* accepted) {
+int hx_lws_warm_start(hx_ctx* c, const float* params, int32_t p_step, int32_t* accepted) {
     HX_ST(check_qp(c));
     if (!params) return HX_EINVAL;
     if (accepted) *accepted = 0;
@@ -1067,8 +1067,19 @@ int hx_lws_warm_start(hx_ctx* c, const float* params, int32_t* accepted) {
     // x_tmp = [project(q') | p]
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_f2d(qf, nq, qof(c->xt), c->st));
     HX_LAUNCH(HX_KIND_OTHER, 1, launch_step_q(qof(c->xt), nullptr, c->K, c->I, c->eps, qof(c->xt), c->st));
-    HX_CK(cudaMemcpyAsync(pof(c, c->xt), pof(c, c->x), (size_t)c->K * 4 * c->J * sizeof(double),
-                          cudaMemcpyDeviceToDevice, c->st));
+    if (p_step) {
+        // x_tmp.p = one P step at (q', p) (update_p!, src/algorithms_inner.jl:224-355);
+        // x_next.p holds the QP's step (x_next is rewritten by the next iteration)
+        HX_ST(pass_p(c, qof(c->xt), pof(c, c->x), true, c->XtXp, c->Xtzp));
+        HX_LAUNCH(HX_KIND_QP_P, 1,
+                  launch_qp_p(c->K, c->J, c->XtXp, c->Xtzp, pof(c, c->x), c->rho, pof(c, c->xn), c->slots, c->qp_ws,
+                              c->st, c->lo.penalty == 0));
+        HX_LAUNCH(HX_KIND_OTHER, 1,
+                  launch_step_p(pof(c, c->x), pof(c, c->xn), c->K, c->J, c->eps, pof(c, c->xt), c->st));
+    } else {
+        HX_CK(cudaMemcpyAsync(pof(c, c->xt), pof(c, c->x), (size_t)c->K * 4 * c->J * sizeof(double),
+                              cudaMemcpyDeviceToDevice, c->st));
+    }
     HX_ST(loglik_to_slot(c, qof(c->x), pof(c, c->x), S_TMP));
     HX_ST(read_slots(c));
     const double ll0 = c->h_slots[S_TMP];

@@ -75,17 +75,23 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* m) {
 }
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-// Bounded wait for the phase with the given parity; false on timeout.
+// Bounded wait for the phase with the given parity; false on timeout.  The
+// first probe does not block (test_wait); the blocking probes (try_wait, which
+// may suspend the thread for a while by itself) run only while the budget
+// lasts, so a phase still open after budget_cycles always fails the wait.
 __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, long long budget_cycles) {
     const uint32_t addr = smem_u32(m);
+    uint32_t done;
+    asm volatile("{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+    if (done) return true;
     const long long t0 = clock64();
-    for (;;) {
-        uint32_t done;
+    while (clock64() - t0 <= budget_cycles) {
         asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
                      : "=r"(done) : "r"(addr), "r"(parity) : "memory");
         if (done) return true;
-        if (clock64() - t0 > budget_cycles) return false;
     }
+    return false;
 }
 
 template <int NCOLS>

@@ -56,7 +56,7 @@ SIGNATURES = {
     "hx_lws_forward": (I32, [P, C.c_int64, I32, P, P, P]),
     "hx_lws_grad": (I32, [P, P, C.c_int64, I32, P, P, P, P]),
     "hx_lws_train": (I32, [P, P, C.c_int64, I32, P, P, P, I32, C.c_int64, C.c_float, C.c_uint64, I32, P, P]),
-    "hx_lws_warm_start": (I32, [P, P, C.POINTER(I32)]),
+    "hx_lws_warm_start": (I32, [P, P, I32, C.POINTER(I32)]),
     "hx_fit_many": (I32, [C.POINTER(P), I32, I32, C.c_double, I32, I32, C.POINTER(HxFitInfo), C.POINTER(I32)]),
     "hx_set_loop_opts": (I32, [P, C.POINTER(HxLoopOpts)]),
     "hx_status_string": (C.c_char_p, [I32]),

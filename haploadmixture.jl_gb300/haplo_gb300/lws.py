@@ -120,16 +120,17 @@ def train(feat, target, params=None, steps=2000, batch=8192, lr=2e-3, seed=1, lo
     return P.cpu().numpy(), losses[:steps].cpu().numpy()
 
 
-def warm_start(d, params):
-    """Replaces Q by the network's prediction when that raises the
-    log-likelihood (hx_lws_warm_start); returns True if it did."""
+def warm_start(d, params, p_step=False):
+    """Replaces Q by the network's prediction (and, with p_step, P by one P
+    step at that Q) when that raises the log-likelihood
+    (hx_lws_warm_start); returns True if it did."""
     acc = C.c_int32()
     P = np.ascontiguousarray(params, dtype=np.float32)
-    d._ck(d.lib.hx_lws_warm_start(d._h, P.ctypes.data_as(C.c_void_p), C.byref(acc)))
+    d._ck(d.lib.hx_lws_warm_start(d._h, P.ctypes.data_as(C.c_void_p), int(p_step), C.byref(acc)))
     return bool(acc.value)
 
 
-def fit(d, params=None, n_iter=1000, rtol=1e-7, em_iters=5, plain_iters=3):
+def fit(d, params=None, n_iter=1000, rtol=1e-7, em_iters=5, plain_iters=3, p_step=False):
     """The chosen fit: init_em!, `plain_iters` outer iterations, the warm start,
     then admixture_qn! to convergence (from a fresh QN history when the warm
     start was kept, else continuing the plain loop unchanged).  Returns the fit
@@ -137,10 +138,10 @@ def fit(d, params=None, n_iter=1000, rtol=1e-7, em_iters=5, plain_iters=3):
     time."""
     t0 = time.time()
     d.init_em(em_iters)
-    i1 = d.admixture_qn(n_iter=plain_iters, rtol=rtol)
+    i1 = d.admixture_qn(n_iter=plain_iters, rtol=rtol) if plain_iters > 0 else {"converged": 0, "iters": 0}
     accepted = False
     if not i1["converged"]:
-        accepted = warm_start(d, load_params() if params is None else params)
+        accepted = warm_start(d, load_params() if params is None else params, p_step=p_step)
         if accepted:
             i2 = d.admixture_qn(n_iter=n_iter - i1["iters"], rtol=rtol)
         else:
@@ -153,12 +154,31 @@ def fit(d, params=None, n_iter=1000, rtol=1e-7, em_iters=5, plain_iters=3):
     return info
 
 
+def align_labels(p_now, p_conv):
+    """Ancestry permutation perm with p_conv[perm[k]] closest to p_now[k]
+    (least total L1 distance between the K x 4J haplotype-frequency rows; an
+    assignment problem, solved exactly).  The fit's labelling of ancestries is
+    arbitrary and can still change after the point where features are taken,
+    so a converged Q is only a target once its rows are put in the labelling
+    of that point: target[k] = q_conv[perm[k]]."""
+    from scipy.optimize import linear_sum_assignment
+    cost = np.abs(p_now[:, None, :] - p_conv[None, :, :]).sum(axis=2)
+    rows, cols = linear_sum_assignment(cost)
+    perm = np.empty(p_now.shape[0], dtype=np.int64)
+    perm[rows] = cols
+    return perm
+
+
 def training_set(cohorts=50, I=20000, J=5000, K=6, seed=20261209, em_iters=5, plain_iters=3, rtol=1e-7,
-                 precision="mixed", verbose=False):
+                 precision="mixed", align=True, verbose=False, stats=None, q_now_out=None):
     """(features, converged Q) pairs from the method's own fits on simulated
     cohorts: alpha in [0.1, 1], differentiation mix in [0.05, 0.5]; features
     are taken where the warm start applies (after init_em! and plain_iters
-    outer iterations)."""
+    outer iterations).  With align, each converged Q is permuted into the
+    ancestry labelling of that point (align_labels on P).  stats (a list), if
+    given, receives per cohort the share of individuals whose largest Q entry
+    is the same ancestry at that point and at convergence, before and after
+    the alignment."""
     torch = _torch()
     from . import synth
     rng = np.random.default_rng(seed)
@@ -175,10 +195,21 @@ def training_set(cohorts=50, I=20000, J=5000, K=6, seed=20261209, em_iters=5, pl
                        bed_on_device=True)
         d.set_qp(*random_init(I, J, K, np.random.default_rng(seed + 7 * c)))
         d.init_em(em_iters)
-        d.admixture_qn(n_iter=plain_iters, rtol=rtol)
+        if plain_iters > 0:
+            d.admixture_qn(n_iter=plain_iters, rtol=rtol)
         f = features(d)
+        q_now, p_now = d.get_qp()
         d.admixture_qn(n_iter=1000, rtol=rtol, iter_count_offset=plain_iters)
-        q = d.get_qp()[0].T.astype(np.float32)       # (I, K)
+        q_conv, p_conv = d.get_qp()
+        perm = align_labels(p_now, p_conv) if align else np.arange(K)
+        q = q_conv[perm].T.astype(np.float32)        # (I, K), labelling of the feature point
+        if q_now_out is not None:
+            q_now_out.append(q_now.T.astype(np.float32))
+        if stats is not None:
+            a_now = q_now.argmax(axis=0)
+            stats.append({"agree_unaligned": float(np.mean(a_now == q_conv.argmax(axis=0))),
+                          "agree_aligned": float(np.mean(a_now == q.argmax(axis=1))),
+                          "perm": perm.tolist()})
         feats.append(f)
         targets.append(q)
         if verbose:

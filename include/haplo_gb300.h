@@ -227,11 +227,12 @@ int hx_lws_grad(const float* d_feat, const float* d_target, int64_t n, int32_t K
 int hx_lws_train(const float* d_feat, const float* d_target, int64_t n, int32_t K, float* d_params, float* d_m,
                  float* d_v, int32_t steps, int64_t batch, float lr, uint64_t seed, int32_t step0, double* d_losses,
                  void* stream);
-/* Warm start: Q' = project(network(features of the current state)) replaces Q
- * if it raises the log-likelihood at the current P; then the QN history is
+/* Warm start: Q' = project(network(features of the current state)); with
+ * p_step, P' = one P step (update_p!) at (Q', P), else P' = P.  (Q', P')
+ * replaces the state if it raises the log-likelihood; then the QN history is
  * reset (hx_set_qp semantics).  params: host, HX_LWS_NPARAM floats.
- * *accepted (optional) = 1 if Q was replaced. */
-int hx_lws_warm_start(hx_ctx* ctx, const float* params, int32_t* accepted);
+ * *accepted (optional) = 1 if the state was replaced. */
+int hx_lws_warm_start(hx_ctx* ctx, const float* params, int32_t p_step, int32_t* accepted);
 int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int32_t em_iters, int32_t threads,
                 hx_fit_info* infos, int32_t* status);
 

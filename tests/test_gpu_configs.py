@@ -14,7 +14,11 @@ blocks), K = 5, P = 0.8 shared ancestral + 0.2 Dirichlet noise, 1% missing,
 Q uniform with random jitter.  Census and double-missing counts bit-exact;
 log-likelihood, Q and P gradients and Hessians within 1e-10 relative (to the
 largest entry) at identical Q, P.  The tensor-core passes of the mixed method
-at the same point: gradient 1e-6, Hessian 1e-4.
+at the same point: Hessian 1e-4, gradient 2e-6.  The gradient bound is the
+accumulation bias of the tensor core: each TMEM window takes 16 MMA adds per
+column (8 stages x 2 k-steps) before it is folded, and every add rounds the
+FP32 accumulator toward zero, up to 2^-23 of it: 16 x 2^-23 = 1.9e-6 (the
+measured error here is about 1.1e-6, all of one sign).
 """
 import numpy as np
 import pytest
@@ -120,8 +124,8 @@ def test_c2_mixed_tensor_core_passes(hx, O, c2):
     assert d.loglikelihood(q, p) == pytest.approx(ref["ll"], rel=1e-8)
     XtX, Xtz = d.update_q_accum(q, p)
     oX, oz = ref["q"]
-    assert rel_err(Xtz, oz) < 1e-6 and rel_err(XtX, oX) < 1e-4
+    assert rel_err(Xtz, oz) < 2e-6 and rel_err(XtX, oX) < 1e-4
     XtX, Xtz = d.update_p_accum(q, p)
     oX, oz = ref["p"]
-    assert rel_err(Xtz, oz) < 1e-6 and rel_err(XtX, oX) < 1e-4
+    assert rel_err(Xtz, oz) < 2e-6 and rel_err(XtX, oX) < 1e-4
     d.close()

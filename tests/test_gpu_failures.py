@@ -2,12 +2,14 @@
 .bed front end end to end.
 
 * Bounded waits: with a one-cycle wait budget (hx_set_wait_budget) a
-  tensor-core pass stops at its first pipeline wait, drains what it issued
-  and the call returns HX_ETIMEOUT; the same handle then runs the pass again
+  tensor-core pass stops at the first pipeline wait whose phase is still
+  open (at the latest the wait for the last window's MMAs), drains what it
+  issued and the call returns HX_ETIMEOUT; the same handle then runs the pass again
   with the default budget and matches the oracle (gradient 1e-6, Hessian
   1e-4 relative to the largest entry, the tensor-core bounds of
   test_gpu_tc.py).
-* Host-side refusals: NaN in the host Q, out-of-range sizes.
+* Host-side refusals: K beyond HX_KMAX, a SNP range beyond the matrix, a
+  fit with no Q/P set.
 * run_admixture (src/driver.jl:38-79) on a .bed written to disk that holds
   more individuals and SNPs than the fit uses: the FP64 fit equals the
   oracle fit on the same bytes (ll 1e-9 relative, Q and P 1e-5, +-1 outer
@@ -35,7 +37,10 @@ def _make(hx, c, precision):
 def test_wait_timeout_returns_status_and_handle_recovers(hx, O, side):
     from haplo_gb300 import _lib
     from haplo_gb300.admix import random_init
-    c = small_cohort(300, 61, 4, seed=41)
+    # enough blocks that the P side's grid fills its waves with few chunks,
+    # so that each CTA runs many stages (its waits on earlier MMAs then meet
+    # open phases)
+    c = small_cohort(1000, 80000, 4, seed=41)
     b = O.Bed(c["bed"], c["I"], c["J"])
     q, p = random_init(c["I"], c["J"], c["K"], np.random.default_rng(5))
     d = _make(hx, c, "mixed")
