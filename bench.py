@@ -65,6 +65,9 @@ def parse(argv=None):
                     help="time one EM and one outer iteration of the plain FP64 method instead of fitting it "
                          "to convergence (the default, about 11 minutes at I=1e5, J=1e5, K=8)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-full-fit", action="store_true",
+                    help="also fit the whole cohort with the CPU oracle from the same start (measured, not "
+                         "extrapolated; hours at I=1e5, J=1e5; minutes at I=1e4, J=5e4)")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--cpu-slice-blocks", type=int, default=0)
     return ap.parse_args(argv)
@@ -483,6 +486,20 @@ def run_ours(args, world, rank, local):
                       "scaled by J/%d; I-only pieces (per-individual QPs, projections) and the ZAL point at full "
                       "size; summed with this fit's %d EM + %d outer iterations (extrapolated)"
                       % (threads, I, Js, Js, args.em_iters, iters)}
+    if args.cpu_full_fit and rank == 0:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        hb = bed_dev.cpu().numpy().reshape(n_snp, bps)
+        b = O.Bed(hb, I, J)
+        t0 = time.perf_counter()
+        oq, op, oll, oit, _ = O.fit(b, K, q0, p0, n_iter=args.n_iter, rtol=args.rtol, em_iters=args.em_iters,
+                                    threads=threads)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_full_fit"] = {
+            "value": t_cpu, "unit": "s", "cores": threads, "kind": "port", "host": cpu_info(), "extrapolated": False,
+            "outer_iters": oit, "loglik": oll, "speedup_chosen_vs_cpu": t_cpu / (ms / 1e3),
+            "chosen_vs_cpu": {"ll_rel_diff": abs(ll - oll) / abs(oll), "q_max_abs_diff": float(np.abs(q_c - oq).max())},
+            "sample": "oracle port: the whole fit (init_em! + admixture_qn! to rtol) from the GPU fits' start"}
     d.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -130,12 +130,18 @@ def warm_start(d, params, p_step=False):
     return bool(acc.value)
 
 
-def fit(d, params=None, n_iter=1000, rtol=1e-7, em_iters=5, plain_iters=3, p_step=False):
-    """The chosen fit: init_em!, `plain_iters` outer iterations, the warm start,
-    then admixture_qn! to convergence (from a fresh QN history when the warm
-    start was kept, else continuing the plain loop unchanged).  Returns the fit
-    info with the total outer iterations, 'warm_start_accepted' and the wall
-    time."""
+def fit(d, params=None, n_iter=1000, rtol=1e-7, em_iters=5, plain_iters=1, p_step=True):
+    """The warm-started fit: init_em!, `plain_iters` outer iterations, the warm
+    start (the network's Q and, with p_step, one P step at it, kept only if
+    that raises the log-likelihood), then admixture_qn! to convergence (from a
+    fresh QN history when the warm start was kept, else continuing the plain
+    loop unchanged).  Returns the fit info with the total outer iterations,
+    'warm_start_accepted' and the wall time.
+
+    Without the P step the network's Q is judged at the current P, where the
+    current Q (just optimised for that P by the Q step) is hard to beat, and
+    after 3 outer iterations it was never kept; one iteration in, with the P
+    step, it is kept on most cohorts."""
     t0 = time.time()
     d.init_em(em_iters)
     i1 = d.admixture_qn(n_iter=plain_iters, rtol=rtol) if plain_iters > 0 else {"converged": 0, "iters": 0}
@@ -169,7 +175,7 @@ def align_labels(p_now, p_conv):
     return perm
 
 
-def training_set(cohorts=50, I=20000, J=5000, K=6, seed=20261209, em_iters=5, plain_iters=3, rtol=1e-7,
+def training_set(cohorts=50, I=20000, J=5000, K=6, seed=20261209, em_iters=5, plain_iters=1, rtol=1e-7,
                  precision="mixed", align=True, verbose=False, stats=None, q_now_out=None):
     """(features, converged Q) pairs from the method's own fits on simulated
     cohorts: alpha in [0.1, 1], differentiation mix in [0.05, 0.5]; features
@@ -262,6 +268,7 @@ def _main():
     t.add_argument("--steps", type=int, default=3000)
     t.add_argument("--batch", type=int, default=8192)
     t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--plain-iters", type=int, default=1)
     t.add_argument("--out", default=PARAMS_PATH)
     e = sub.add_parser("eval")
     e.add_argument("--config", default="C5")
@@ -272,7 +279,7 @@ def _main():
         _evaluate(a)
         return
     t0 = time.time()
-    X, T = training_set(cohorts=a.cohorts, I=a.I, J=a.J, K=a.K, verbose=True)
+    X, T = training_set(cohorts=a.cohorts, I=a.I, J=a.J, K=a.K, plain_iters=a.plain_iters, verbose=True)
     t1 = time.time()
     params, losses = train(X, T, steps=a.steps, batch=a.batch, lr=a.lr, log_every=max(a.steps // 10, 1))
     t2 = time.time()

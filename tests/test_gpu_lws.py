@@ -67,13 +67,38 @@ def test_training_reduces_the_loss_and_is_reproducible(hx):
     assert np.mean(l1[-20:]) - ent < 0.5 * (np.mean(l1[:5]) - ent)
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
-                                                    "haploadmixture.jl_gb300", "haplo_gb300", "lws_params.npy")),
-                    reason="trained parameters not present")
+PARAMS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "haploadmixture.jl_gb300",
+                      "haplo_gb300", "lws_params.npy")
+
+
+def _xent(pred, target):
+    return float(-np.mean(np.sum(target * np.log(np.clip(pred, 1e-12, None)), axis=1)))
+
+
+@pytest.mark.skipif(not os.path.exists(PARAMS), reason="trained parameters not present")
+def test_network_gain_as_a_predictor(hx):
+    """What the trained network gains, on held-out cohorts (seeds outside the
+    training set), where the warm start applies (after init_em! and one outer
+    iteration): its Q is closer to the converged Q (cross-entropy, converged
+    rows put in the labelling of that point) than the uniform Q is, by at
+    least 0.02 nats.  The cross-entropy of the fit's own Q at that point is
+    reported beside it."""
+    from haplo_gb300 import lws
+    qnow = []
+    X, T = lws.training_set(cohorts=3, I=20000, J=5000, K=6, seed=4242, plain_iters=1, q_now_out=qnow)
+    pred = lws.forward(X, lws.load_params())
+    x_net, x_uni = _xent(pred, T), _xent(np.full_like(T, 1.0 / T.shape[1]), T)
+    x_cur, x_floor = _xent(np.concatenate(qnow), T), _xent(T, T)
+    print("cross-entropy vs converged Q: network %.4f, uniform %.4f, current Q %.4f, targets' entropy %.4f"
+          % (x_net, x_uni, x_cur, x_floor))
+    assert x_net < x_uni - 0.02
+
+
+@pytest.mark.skipif(not os.path.exists(PARAMS), reason="trained parameters not present")
 def test_warm_started_fit_reaches_the_plain_optimum(hx):
-    """Held-out cohort (seed outside the training set): the chosen fit (with the
-    warm start) and the plain mixed fit converge to the same log-likelihood;
-    the iteration counts of both are reported."""
+    """Held-out cohort: the warm-started fit ends at the plain mixed fit's
+    log-likelihood or above it (within 1e-8 relative; the fit maximises it);
+    the iteration counts and times of both are reported."""
     from haplo_gb300 import lws, synth
     from haplo_gb300.admix import random_init
     I, J, K = 6000, 2000, 6
@@ -90,4 +115,4 @@ def test_warm_started_fit_reaches_the_plain_optimum(hx):
     ic = lws.fit(chosen, n_iter=500, rtol=1e-9, em_iters=5)
     print("plain iters %d ll %.10e %.3f s | warm start accepted %s iters %d ll %.10e %.3f s"
           % (ip["iters"], ip["ll"], ip["seconds"], ic["warm_start_accepted"], ic["iters"], ic["ll"], ic["seconds"]))
-    assert ic["ll"] == pytest.approx(ip["ll"], rel=1e-8)
+    assert ic["ll"] >= ip["ll"] - 1e-8 * abs(ip["ll"])
