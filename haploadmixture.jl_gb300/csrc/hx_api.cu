@@ -16,6 +16,9 @@
 #include <algorithm>
 #include <atomic>
 #include <thread>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 using namespace hx;
 
@@ -47,6 +50,9 @@ struct hx_ctx {
     int S_ll = 1, wpc_ll = 1;                // FP32 log-likelihood pass
     bool tc = false;                         // Hessian passes on the tensor cores
     int S_qt = 1, wpc_qt = 2, S_pt = 1, ipc_pt = 64;
+    // chunk counts the partial buffers hold: twice the plan's, the range the
+    // autotuner tries (hx_autotune)
+    int Sq_cap = 1, Sp_cap = 1, Sll_cap = 1;
     bool have_qp = false;
     long long wait_budget = HX_WAIT_BUDGET_DEFAULT;   // tensor-core pipeline waits (clock64 cycles)
     std::string err;
@@ -145,6 +151,33 @@ int64_t pick_chunk(int64_t tiles, int64_t units, int64_t slots, int64_t waves) {
     return best;
 }
 
+// Chunk lengths (grid.y splits) of the mixed method's three pass kernels that
+// hx_autotune measured fastest, per device, K, I and J, for the whole process.
+struct TuneVal { int wpc_qt, spc_pt, wpc_ll; };
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int64_t, int64_t>, TuneVal> g_tune;
+
+bool tune_lookup(const hx_ctx* c, TuneVal& v) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune.find(std::make_tuple(c->device, c->K, c->I, c->J));
+    if (it == g_tune.end()) return false;
+    v = it->second;
+    return true;
+}
+void tune_store(const hx_ctx* c, const TuneVal& v) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune[std::make_tuple(c->device, c->K, c->I, c->J)] = v;
+}
+void apply_tuned(hx_ctx* c, const TuneVal& v) {
+    const int64_t nst = (c->I + 31) / 32;
+    c->wpc_qt = v.wpc_qt;
+    c->S_qt = (c->JW + v.wpc_qt - 1) / v.wpc_qt;
+    c->ipc_pt = v.spc_pt * 32;
+    c->S_pt = (int)((nst + v.spc_pt - 1) / v.spc_pt);
+    c->wpc_ll = v.wpc_ll;
+    c->S_ll = (c->JW + v.wpc_ll - 1) / v.wpc_ll;
+}
+
 void plan(hx_ctx* c) {
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
@@ -173,6 +206,13 @@ void plan(hx_ctx* c) {
     const int64_t tilesL = loglik_f32x2_blocks(c->Ipad, c->K);
     c->wpc_ll = (int)pick_chunk(tilesL, c->JW, (int64_t)nsm * loglik_f32x2_resident(c->K), 8);
     c->S_ll = (c->JW + c->wpc_ll - 1) / c->wpc_ll;
+    c->Sq_cap = std::min(c->JW, 2 * c->S_qt);
+    c->Sp_cap = (int)std::min<int64_t>(nst, 2 * (int64_t)c->S_pt);
+    c->Sll_cap = std::min(c->JW, 2 * c->S_ll);
+    // chunk lengths an earlier hx_autotune chose for this shape (always
+    // within the caps above, which depend on the shape only)
+    TuneVal tv;
+    if (c->tc && tune_lookup(c, tv)) apply_tuned(c, tv);
 }
 
 PassArgs pass_args(hx_ctx* c, const double* q, const double* p) {
@@ -450,11 +490,12 @@ int create_common(const uint8_t* bed, bool bed_on_device, int64_t bps, int64_t n
     HX_ST(dalloc(c, &c->Xtzq, (size_t)K * I));
     HX_ST(dalloc(c, &c->XtXp, (size_t)K * K * 4 * J));
     HX_ST(dalloc(c, &c->Xtzp, (size_t)K * 4 * J));
-    HX_ST(dalloc(c, &c->part_q, (size_t)std::max(c->S_q, c->tc ? c->S_qt : 1) * NVmax * c->Ipad));
-    const int Sp_max = std::max(c->S_p, c->tc ? c->S_pt : 1);
+    HX_ST(dalloc(c, &c->part_q, (size_t)std::max(c->S_q, c->tc ? c->Sq_cap : 1) * NVmax * c->Ipad));
+    const int Sp_max = std::max(c->S_p, c->tc ? c->Sp_cap : 1);
     if (Sp_max > 1) HX_ST(dalloc(c, &c->part_p, (size_t)Sp_max * NVmax * 4 * J));
     HX_ST(dalloc(c, &c->part_ll, (size_t)std::max<int64_t>((c->Ipad / ACC_THREADS) * c->S_q,
-                                                            (int64_t)loglik_f32x2_blocks(c->Ipad, K) * c->S_ll)));
+                                                            (int64_t)loglik_f32x2_blocks(c->Ipad, K) *
+                                                                std::max(c->S_ll, c->Sll_cap))));
     HX_ST(dalloc(c, &c->part_qn, (size_t)qn_dots_blocks(c->nx) * (2 * HX_QMAX * HX_QMAX + HX_QMAX)));
     HX_ST(dalloc(c, &c->coef, HX_QMAX));
     HX_ST(dalloc(c, &c->slots, HX_NSLOT));
@@ -1104,6 +1145,81 @@ int hx_fit(hx_ctx* c, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_info
         info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return HX_OK;
+}
+
+// Measures each of the mixed method's pass kernels (Q and P tensor-core
+// passes with their reductions, FP32 log-likelihood) at the current state
+// for chunk counts from half to twice the plan's, keeps the fastest, and
+// remembers it for every later context of the same device and shape.
+int hx_autotune(hx_ctx* c, int32_t* chunks) {
+    HX_ST(check_qp(c));
+    if (!c->tc) return HX_OK;
+    HX_CK(cudaSetDevice(c->device));
+    const double* q = qof(c->x);
+    const double* p = pof(c, c->x);
+    auto elapsed = [&](auto&& run, float& best) -> int {
+        best = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+            HX_CK(cudaEventRecord(c->ev0, c->st));
+            HX_ST(run());
+            HX_CK(cudaEventRecord(c->ev1, c->st));
+            HX_CK(cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            HX_CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            best = std::min(best, ms);
+        }
+        return HX_OK;
+    };
+    // candidate chunk lengths: chunk counts S0 * f for f in [1/2, 2], within the cap
+    auto candidates = [](int64_t units, int S0, int cap) {
+        std::vector<int64_t> per;
+        for (double f : {0.5, 2.0 / 3.0, 0.75, 1.0, 4.0 / 3.0, 1.5, 2.0}) {
+            int64_t S = std::max<int64_t>(1, std::min<int64_t>(cap, (int64_t)std::lround(S0 * f)));
+            const int64_t len = (units + S - 1) / S;
+            if (std::find(per.begin(), per.end(), len) == per.end()) per.push_back(len);
+        }
+        return per;
+    };
+    const int64_t nst = (c->I + 31) / 32;
+    TuneVal best{c->wpc_qt, c->ipc_pt / 32, c->wpc_ll};
+    float t_best = 0.f, t = 0.f;
+    // Q side
+    {
+        const TuneVal keep = best;
+        HX_ST(elapsed([&] { return pass_q(c, q, p, true, c->XtXq, c->Xtzq); }, t_best));
+        for (int64_t len : candidates(c->JW, c->S_qt, c->Sq_cap)) {
+            apply_tuned(c, TuneVal{(int)len, keep.spc_pt, keep.wpc_ll});
+            HX_ST(elapsed([&] { return pass_q(c, q, p, true, c->XtXq, c->Xtzq); }, t));
+            if (t < t_best) { t_best = t; best.wpc_qt = (int)len; }
+        }
+        apply_tuned(c, best);
+    }
+    // P side
+    {
+        HX_ST(elapsed([&] { return pass_p(c, q, p, true, c->XtXp, c->Xtzp); }, t_best));
+        const TuneVal keep = best;
+        for (int64_t len : candidates(nst, c->S_pt, c->Sp_cap)) {
+            apply_tuned(c, TuneVal{keep.wpc_qt, (int)len, keep.wpc_ll});
+            HX_ST(elapsed([&] { return pass_p(c, q, p, true, c->XtXp, c->Xtzp); }, t));
+            if (t < t_best) { t_best = t; best.spc_pt = (int)len; }
+        }
+        apply_tuned(c, best);
+    }
+    // log-likelihood
+    {
+        HX_ST(elapsed([&] { return loglik_to_slot(c, q, p, S_TMP); }, t_best));
+        const TuneVal keep = best;
+        for (int64_t len : candidates(c->JW, c->S_ll, c->Sll_cap)) {
+            apply_tuned(c, TuneVal{keep.wpc_qt, keep.spc_pt, (int)len});
+            HX_ST(elapsed([&] { return loglik_to_slot(c, q, p, S_TMP); }, t));
+            if (t < t_best) { t_best = t; best.wpc_ll = (int)len; }
+        }
+        apply_tuned(c, best);
+    }
+    tune_store(c, best);
+    if (chunks) { chunks[0] = c->S_qt; chunks[1] = c->S_pt; chunks[2] = c->S_ll; }
+    HX_ST(read_slots(c));
+    return take_timeout(c);
 }
 
 int hx_set_profiling(hx_ctx* c, int32_t on) {

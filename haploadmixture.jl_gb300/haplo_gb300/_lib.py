@@ -77,6 +77,7 @@ SIGNATURES = {
     "hx_update_p_accum": (I32, [P, P, P, P, P]),
     "hx_em_p_accum": (I32, [P, P, P, P]),
     "hx_set_wait_budget": (I32, [P, I64]),
+    "hx_autotune": (I32, [P, P]),
     "hx_qp_q": (I32, [P, I64, P, P, P, P]),
     "hx_qp_p": (I32, [P, I64, P, P, P, P]),
     "hx_project_q": (I32, [P, I64, P]),

@@ -229,6 +229,14 @@ class GB300Admix:
         with status HX_ETIMEOUT and leaves the handle usable."""
         self._ck(self.lib.hx_set_wait_budget(self._h, int(cycles)))
 
+    def autotune(self):
+        """hx_autotune: picks the fastest grid splits of the mixed method's
+        pass kernels at the current Q/P; returns the chunk counts (Q pass, P
+        pass, log-likelihood)."""
+        ch = np.zeros(3, dtype=np.int32)
+        self._ck(self.lib.hx_autotune(self._h, ptr(ch)))
+        return tuple(int(x) for x in ch)
+
     def update_q_accum(self, q, p):
         qa, pa = _fortran(q, (self.K, self.I)), _fortran(p, (self.K, 4 * self.J))
         XtX = np.empty((self.K, self.K, self.I), order="F")

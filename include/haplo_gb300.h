@@ -236,6 +236,17 @@ int hx_lws_warm_start(hx_ctx* ctx, const float* params, int32_t p_step, int32_t*
 int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int32_t em_iters, int32_t threads,
                 hx_fit_info* infos, int32_t* status);
 
+/* Tile-shape autotuner of the mixed method (no reference counterpart): times
+ * the Q and P tensor-core passes and the FP32 log-likelihood pass at the
+ * context's current Q/P for chunk counts (grid splits along the reduction)
+ * from half to twice the planned ones, keeps the fastest for this context,
+ * and applies it to every later context of the same device, K, I and J in
+ * this process (hx_create, hx_create_shared).  A different chunking only
+ * reorders the FP32/FP64 partial sums.  chunks (optional, 3 entries)
+ * receives the chosen chunk counts (Q pass, P pass, log-likelihood).  No-op
+ * (HX_OK) for the plain FP64 method and the CUDA-core path. */
+int hx_autotune(hx_ctx* ctx, int32_t* chunks);
+
 /* ---- launch accounting (no counterpart in the reference, which prints
  * @time per phase, src/algorithms_inner.jl:114,135,241,259) ---- */
 #define HX_KIND_ACCUM_Q 0  /* Q-side gradient+Hessian pass */

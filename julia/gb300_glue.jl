@@ -241,6 +241,14 @@ function gb300_double_missing(d_cu::GB300Admix)
     dm
 end
 
+# grid splits of the mixed method's pass kernels, measured at the current Q/P
+# (set them first, e.g. with gb300_set_qp!); later handles of the shape reuse them
+function gb300_autotune!(d_cu::GB300Admix)
+    chunks = zeros(Int32, 3)
+    hxcheck(d_cu.ptr, ccall((:hx_autotune, libhx), Cint, (Ptr{Cvoid}, Ptr{Int32}), d_cu.ptr, chunks))
+    chunks
+end
+
 function gb300_set_wait_budget!(d_cu::GB300Admix, cycles::Integer)
     hxcheck(d_cu.ptr, ccall((:hx_set_wait_budget, libhx), Cint, (Ptr{Cvoid}, Int64), d_cu.ptr, cycles))
 end

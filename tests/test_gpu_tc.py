@@ -93,3 +93,29 @@ def test_tc_fit_reaches_fp64_optimum(hx, O):
 @pytest.fixture(scope="module")
 def coh_tc():
     return small_cohort(1000, 500, 6, seed=77, miss=0.02)
+
+
+def test_autotune_keeps_the_sums(hx, O):
+    """hx_autotune picks grid splits by timing; the sums it leaves behind are
+    the tensor-core pass's to the same bounds (gradient 1e-6, Hessian 1e-4,
+    log-likelihood 1e-8), and a later context of the same shape runs with
+    them (its sums equal the tuned context's bit for bit)."""
+    from haplo_gb300.admix import random_init
+    c = small_cohort(2304, 901, 5, seed=77)      # a shape no other test uses
+    b = O.Bed(c["bed"], c["I"], c["J"])
+    q, p = random_init(c["I"], c["J"], c["K"], np.random.default_rng(8))
+    d = make(hx, c, precision="mixed")
+    d.set_qp(q, p)
+    chunks = d.autotune()
+    assert len(chunks) == 3 and min(chunks) >= 1
+    XtX, Xtz = d.update_q_accum(q, p)
+    oX, oz = O.accum_q(b, c["K"], q, p)
+    assert rel_err(Xtz, oz) < 1e-6 and rel_err(XtX, oX) < 1e-4
+    XtXp, Xtzp = d.update_p_accum(q, p)
+    oXp, ozp = O.accum_p(b, c["K"], q, p)
+    assert rel_err(Xtzp, ozp) < 1e-6 and rel_err(XtXp, oXp) < 1e-4
+    assert d.loglikelihood(q, p) == pytest.approx(O.loglik(b, c["K"], q, p), rel=1e-8)
+    d2 = make(hx, c, precision="mixed")
+    X2, z2 = d2.update_q_accum(q, p)
+    np.testing.assert_array_equal(X2, XtX)
+    np.testing.assert_array_equal(d2.update_p_accum(q, p)[1], Xtzp)
