@@ -1,4 +1,4 @@
-"""Learned warm start of Q (BASELINE configuration 5; no reference counterpart).
+"""Learned warm start of Q (no reference counterpart).
 
 A small permutation-equivariant network maps, for each individual, the
 per-ancestry block log-likelihood sums and the Q gradient at the current state

@@ -1,5 +1,5 @@
-"""K sweep with random restarts on one GPU (BASELINE configuration C4 shape:
-K = 2..10 x 4 restarts on one cohort).
+"""K sweep with random restarts on one GPU (for example K = 2..10 x 4
+restarts on one cohort of I = 20,000 individuals x 40,000 SNPs).
 
 The reference fits one K per run_admixture call (src/driver.jl:38-79) and
 names AIC-based model selection only in its README (README.md:9).  Here all

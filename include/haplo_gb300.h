@@ -200,7 +200,7 @@ int hx_fit(hx_ctx* ctx, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_in
  * hx_fit alone.  status (optional, n entries) receives each fit's status;
  * the return value is the first non-OK status, or HX_OK. */
 int hx_create_shared(const hx_ctx* parent, int32_t K, const hx_opts* opts, hx_ctx** out);
-/* Learned warm start of Q (no reference counterpart; BASELINE configuration 5).
+/* Learned warm start of Q (no reference counterpart).
  * Features of (individual i, ancestry k), two FP32 values each, feat[i][k][2]:
  *   f1 = a_k - max_k' a_k', a_k = (1/n_i) sum_j log L_ij(Q_i = e_k)
  *   f2 = (g - 1) sqrt(n_i), g = Xtz_q[k,i] / (2 n_i) (Q gradient per block),
