@@ -300,7 +300,7 @@ def run_reference(args, world, rank):
         return
     cfg = load_config(args)
     threads = os.cpu_count() or 1
-    Js = min(args.cpu_slice_blocks or 1000, cfg["J"])
+    Js = min(args.cpu_slice_blocks or 500, cfg["J"])
     vals, sample_s = [], []
     for s in range(args.warmup + args.steps):
         j0 = (s * Js) % max(1, cfg["J"] - Js + 1)
