@@ -1151,9 +1151,8 @@ int hx_fit(hx_ctx* c, int32_t n_iter, double rtol, int32_t em_iters, hx_fit_info
 // passes with their reductions, FP32 log-likelihood) at the current state
 // for chunk counts from half to twice the plan's, keeps the fastest, and
 // remembers it for every later context of the same device and shape.
-int hx_autotune(hx_ctx* c, int32_t* chunks) {
-    HX_ST(check_qp(c));
-    if (!c->tc) return HX_OK;
+namespace {
+int autotune(hx_ctx* c, TuneVal& best) {
     HX_CK(cudaSetDevice(c->device));
     const double* q = qof(c->x);
     const double* p = pof(c, c->x);
@@ -1181,7 +1180,6 @@ int hx_autotune(hx_ctx* c, int32_t* chunks) {
         return per;
     };
     const int64_t nst = (c->I + 31) / 32;
-    TuneVal best{c->wpc_qt, c->ipc_pt / 32, c->wpc_ll};
     float t_best = 0.f, t = 0.f;
     // Q side
     {
@@ -1216,10 +1214,24 @@ int hx_autotune(hx_ctx* c, int32_t* chunks) {
         }
         apply_tuned(c, best);
     }
+    return HX_OK;
+}
+}  // namespace
+
+int hx_autotune(hx_ctx* c, int32_t* chunks) {
+    HX_ST(check_qp(c));
+    if (!c->tc) return HX_OK;
+    const TuneVal planned{c->wpc_qt, c->ipc_pt / 32, c->wpc_ll};
+    TuneVal best = planned;
+    int st = autotune(c, best);
+    if (st == HX_OK) st = take_timeout(c);
+    if (st != HX_OK) {          // keep the context on its planned splits
+        apply_tuned(c, planned);
+        return st;
+    }
     tune_store(c, best);
     if (chunks) { chunks[0] = c->S_qt; chunks[1] = c->S_pt; chunks[2] = c->S_ll; }
-    HX_ST(read_slots(c));
-    return take_timeout(c);
+    return HX_OK;
 }
 
 int hx_set_profiling(hx_ctx* c, int32_t on) {
