@@ -139,6 +139,38 @@ __device__ __forceinline__ void pair_eval_tab(unsigned nib, const float qp[4], f
     u[3] = fmaf(hr, qp[0], fmaf(x11, tb.y, x21 * tb.w));
 }
 
+// scale * u of pair_eval_tab (scale a power of two, e.g. 1/4), without the
+// likelihood: the scale is folded into the two reciprocals, and since every
+// later operation is a product or a sum of scaled terms the result has the
+// same bits as u * scale, two multiplications cheaper than scaling u.
+__device__ __forceinline__ void pair_u_tab(unsigned nib, const float qp[4], float u[4], const float4* tab,
+                                           float scale) {
+    const float4 ta = tab[nib & 3u], tb = tab[(nib >> 2) & 3u];
+    const float v10 = fmaf(tb.y, qp[1], tb.x * qp[0]), v11 = fmaf(tb.y, qp[3], tb.x * qp[2]);
+    const float v20 = fmaf(tb.w, qp[1], tb.z * qp[0]), v21 = fmaf(tb.w, qp[3], tb.z * qp[2]);
+    float F1 = fmaf(ta.y, v11, ta.x * v10);
+    float F2 = fmaf(ta.w, v21, ta.z * v20);
+    const bool hh = nib == NIB_HH;
+    const bool mm = nib == NIB_MM;
+    const float den = fmaf(qp[1], qp[2], qp[0] * qp[3]);
+    F1 = hh ? den : F1;
+    F1 = mm ? 1.f : F1;
+    F2 = (hh || mm) ? 1.f : F2;
+    float r1, r2;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(F1));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r2) : "f"(F2));
+    r1 *= scale;
+    r2 *= scale;
+    const float hr = hh ? r1 : 0.f;
+    r1 = (hh || mm) ? 0.f : r1;
+    r2 = (hh || mm) ? 0.f : r2;
+    const float x10 = ta.x * r1, x11 = ta.y * r1, x20 = ta.z * r2, x21 = ta.w * r2;
+    u[0] = fmaf(hr, qp[3], fmaf(x10, tb.x, x20 * tb.z));
+    u[1] = fmaf(hr, qp[2], fmaf(x10, tb.y, x20 * tb.w));
+    u[2] = fmaf(hr, qp[1], fmaf(x11, tb.x, x21 * tb.z));
+    u[3] = fmaf(hr, qp[0], fmaf(x11, tb.y, x21 * tb.w));
+}
+
 // Likelihood only (log-likelihood passes).
 __device__ __forceinline__ float pair_lik_tab(unsigned nib, const float qp[4], const float4* tab) {
     const float4 ta = tab[nib & 3u], tb = tab[(nib >> 2) & 3u];

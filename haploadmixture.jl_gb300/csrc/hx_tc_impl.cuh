@@ -63,6 +63,9 @@ constexpr int A_TILE_PAD = 16 * SBO_PAD;
 // them in FP16's normal range: U * 2^-2 <= 5e4 (U = c/qp <= 2/1e-5); P or Q * 2^12
 // in [0.04, 4096].
 constexpr float U_SCALE = 0.25f;
+// The generators form U * U_SCALE directly and W * U_SCALE beside it (one
+// factor fewer per pair); the Hessian's B rows carry the exact inverse factor.
+constexpr float W_UNDO = 1.0f / U_SCALE;
 constexpr float GB_SCALE = 4096.0f;
 constexpr double G_UNSCALE = 1.0 / 1024.0;
 
@@ -379,7 +382,8 @@ __device__ __forceinline__ void write_b_rows(const float (&v)[8][K], uint8_t* ba
             uint32_t h[4], l[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e)
-                split2(v[2 * e][k] * v[2 * e][k2], v[2 * e + 1][k] * v[2 * e + 1][k2], h[e], l[e]);
+                split2(W_UNDO * (v[2 * e][k] * v[2 * e][k2]), W_UNDO * (v[2 * e + 1][k] * v[2 * e + 1][k2]), h[e],
+                       l[e]);
             put_b_row<K, STACK>(base, kg, tri_idx<K>(k, k2), h, l);
         }
     }
@@ -572,16 +576,13 @@ __device__ __forceinline__ void final_fold(Sync* sy, double* slots, long long bu
 // CTA's q tile by the stage's p tile into a double-buffered 32-column TMEM
 // tile, issued two stages ahead; each thread reads its row's 16 values.
 
-// One pair from its qp: U (scaled) and W.
+// One pair from its qp: U and W, both times U_SCALE.
 template <bool HESS>
 __device__ __forceinline__ void gen_pair_qp(unsigned nib, const float* qp, float* U4, float* W4, const float4* tab) {
-    float L, u[4];
-    pair_eval_tab(nib, qp, L, u, tab);
+    pair_u_tab(nib, qp, U4, tab, U_SCALE);          // U * U_SCALE
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
-        U4[h] = u[h] * U_SCALE;
-        if (HESS) W4[h] = u[h] * rcp_approx(qp[h]);
-    }
+    for (int h = 0; h < 4; ++h)
+        if (HESS) W4[h] = U4[h] * rcp_approx(qp[h]);   // W * U_SCALE
 }
 
 template <int K, bool HESS>
@@ -695,19 +696,25 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
             if (s - 2 + RING < ns) load_stage(s - 2 + RING);
             if (s + QRING < ns) load_qtile(s + QRING);
         }
-        const uint32_t word = SW[slot * 128 + r];
         // this stage's qp: 16 columns of this thread's row.  From stage 2 on it
         // was issued with the MMAs of stage s-2 and is covered by their
         // mma_done, just waited for; stages 0 and 1 wait for the prologue's.
+        // Both loads go out before one wait, with the class word read between.
         float qpv[16];
+        uint32_t word;
         {
             if (s < 2) {
                 const bool ok = __all_sync(0xffffffffu, mbar_wait(&sy->qp_done[b], 0, budget));
                 if (!ok) { set_bad(sy, a.slots); break; }
             }
             fence_after();
-            tmem_ld8(taddr_lane + (uint32_t)(2 * D::WQ + b * 32 + hf * 16), qpv);
-            tmem_ld8(taddr_lane + (uint32_t)(2 * D::WQ + b * 32 + hf * 16 + 8), qpv + 8);
+            uint32_t raw[16];
+            tmem_ld8_async(taddr_lane + (uint32_t)(2 * D::WQ + b * 32 + hf * 16), raw);
+            tmem_ld8_async(taddr_lane + (uint32_t)(2 * D::WQ + b * 32 + hf * 16 + 8), raw + 8);
+            word = SW[slot * 128 + r];
+            tmem_wait_ld();
+#pragma unroll
+            for (int t = 0; t < 16; ++t) qpv[t] = __uint_as_float(raw[t]);
         }
         const uint32_t aB = sA + b * 4 * A_TILE_STD;
 #pragma unroll
@@ -786,8 +793,8 @@ __global__ void __launch_bounds__(TC_THREADS, TcDims<K>::MINB) k_accum_q_tc(Pass
 // CTA: 32 blocks (128 haplotype columns = TMEM lanes) x a chunk of individuals;
 // stage = 32 individuals.  Thread (jl, ig): block jl, individuals 4ig..4ig+3.
 
-// One (individual, block) pair: qp from q and p (4K values), then U (scaled)
-// and W.  qd[k] = (q_k, q_k); pr2[2k] = (p[k,4j], p[k,4j+1]),
+// One (individual, block) pair: qp from q and p (4K values), then U and W,
+// both times U_SCALE.  qd[k] = (q_k, q_k); pr2[2k] = (p[k,4j], p[k,4j+1]),
 // pr2[2k+1] = (p[k,4j+2], p[k,4j+3]): the packed FMAs form qp_h for h pairs
 // in the order of the fmaf chain sum_k q_k p[k,m].
 template <int K, bool HESS>
@@ -802,13 +809,10 @@ __device__ __forceinline__ void gen_pair(unsigned nib, const uint64_t* qd, const
     float qp[4];
     f2_split(z01, qp[0], qp[1]);
     f2_split(z23, qp[2], qp[3]);
-    float L, u[4];
-    pair_eval_tab(nib, qp, L, u, tab);
+    pair_u_tab(nib, qp, U4, tab, U_SCALE);          // U * U_SCALE
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
-        U4[h] = u[h] * U_SCALE;
-        if (HESS) W4[h] = u[h] * rcp_approx(qp[h]);
-    }
+    for (int h = 0; h < 4; ++h)
+        if (HESS) W4[h] = U4[h] * rcp_approx(qp[h]);   // W * U_SCALE
 }
 
 template <int K, bool HESS>
