@@ -339,16 +339,30 @@ class AdmixResult:
         self.I, self.J, self.K = d.I, d.J, d.K
 
 
-def run_admixture(filename, I, J, K, *, rng=None, admix_n_iter=1000, admix_rtol=1e-7, admix_n_em_iters=5,
-                  precision="fp64", Q=3, init_q=None, init_p=None, device=0, verbose=False, return_handle=False):
+def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, skfr_max_inner_iter=50, skfr_seed=0,
+                  admix_n_iter=1000, admix_rtol=1e-7, admix_n_em_iters=5, precision="fp64", Q=3, init_q=None,
+                  init_p=None, device=0, verbose=False, return_handle=False):
     """src/driver.jl:38-79 with the _admixture_base sequence (133-201) on the
     GPU: load the .bed (first I individuals, first 2J SNPs), random start,
     init_em! unless both init_q and init_p are given, then admixture_qn!
-    (mode :ZAL).  Returns (d, clusters, aims) like the reference; clusters
-    and aims are None (no SKFR pre-filter)."""
+    (mode :ZAL).  Returns (d, clusters, aims) like the reference.
+
+    With `sparsity` (the reference's SKFR branch, :60-73 and 84-105), the
+    AIMs are selected first (haplo_gb300.skfr: sparse k-means with feature
+    ranking on blocks of 2 SNPs, `skfr_max_inner_iter` iterations, start from
+    `skfr_seed`), the file is filtered to them as
+    <prefix>_<K>_<2*sparsity>aims.bed, and the fit reads that file; clusters
+    and aims are returned.  Without it they are None."""
     if not str(filename).endswith(".bed"):
         raise ValueError("filename should end with .bed")
     rng = np.random.default_rng(rng) if not isinstance(rng, np.random.Generator) else rng
+    clusters = aims = None
+    if sparsity is not None:
+        from . import skfr
+        data, n_ind, n_snp = bedio.read_bed(filename)
+        clusters, aims, _ = skfr.select_aims(data, n_ind, K, sparsity, seed=skfr_seed,
+                                             max_iter=skfr_max_inner_iter, device=device)
+        filename = skfr.write_filtered(prefix or str(filename)[:-4], data, n_ind, K, aims)
     data, n_ind, n_snp = bedio.read_bed(filename)
     if I > n_ind or 2 * J > n_snp:
         raise ValueError("file has %d individuals and %d SNPs; asked for I=%d, 2J=%d" % (n_ind, n_snp, I, 2 * J))
@@ -367,4 +381,4 @@ def run_admixture(filename, I, J, K, *, rng=None, admix_n_iter=1000, admix_rtol=
     if return_handle:
         return res, d
     d.close()
-    return res, None, None
+    return res, clusters, aims

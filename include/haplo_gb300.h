@@ -236,6 +236,19 @@ int hx_lws_warm_start(hx_ctx* ctx, const float* params, int32_t p_step, int32_t*
 int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int32_t em_iters, int32_t threads,
                 hx_fit_info* infos, int32_t* status);
 
+/* AIM selection before the fit (run_admixture's `sparsity` branch,
+ * src/driver.jl:60-73, 84-105): sparse k-means with feature ranking (SKFR1 of
+ * Zhang, Lange and Xu 2020; the reference calls SparseKmeansFeatureRanking
+ * 0.1.2's sparsekmeans1 on blocks of 2 SNPs) over the first I individuals of
+ * the SNP-major BED matrix (host memory, bytes_per_snp bytes per SNP, n_snp
+ * SNPs; an odd last SNP is ignored).  Genotypes are standardised per SNP
+ * (missing -> mean), the start is k-means++ with uniform draws
+ * SplitMix64(seed + t), and `sparsity` blocks are kept.  Outputs: clusters
+ * (I entries, 0..K-1), aims (2 * sparsity sorted SNP indices), *iters
+ * (optional).  HX_EINVAL for K > I or sparsity outside 1..n_snp/2. */
+int hx_skfr(const uint8_t* bed, int64_t bytes_per_snp, int64_t n_snp, int64_t I, int32_t K, int64_t sparsity,
+            int32_t max_iter, uint64_t seed, int32_t device, int32_t* clusters, int64_t* aims, int32_t* iters);
+
 /* Tile-shape autotuner of the mixed method (no reference counterpart): times
  * the Q and P tensor-core passes and the FP32 log-likelihood pass at the
  * context's current Q/P for chunk counts (grid splits along the reduction)

@@ -290,6 +290,21 @@ function gb300_k_sweep(d_cu::GB300Admix, Ks, restarts::Integer, inits; n_iter=10
     end
 end
 
+# The `sparsity` branch of run_admixture (src/driver.jl:60-73, 84-105): AIM
+# selection by sparse k-means with feature ranking on blocks of 2 SNPs over
+# SnpArray.data; returns (clusters, sorted aims), 1-based like the reference.
+function gb300_skfr(data::AbstractMatrix{UInt8}, I::Integer, K::Integer, sparsity::Integer;
+                    max_iter::Integer=50, seed::Integer=0, device::Integer=0)
+    clusters = zeros(Int32, I)
+    aims = zeros(Int64, 2 * sparsity)
+    iters = Ref{Int32}(0)
+    st = ccall((:hx_skfr, libhx), Cint,
+               (Ptr{UInt8}, Int64, Int64, Int64, Int32, Int64, Int32, UInt64, Int32, Ptr{Int32}, Ptr{Int64}, Ref{Int32}),
+               data, size(data, 1), size(data, 2), I, K, sparsity, max_iter, seed, device, clusters, aims, iters)
+    st == 0 || error("haplo_gb300: hx_skfr: ", unsafe_string(ccall((:hx_status_string, libhx), Cstring, (Cint,), st)))
+    clusters .+ 1, aims .+ 1
+end
+
 # Log-likelihood from device buffers that the caller owns (for example CuArray
 # pointers from CUDA.jl's pool): allocates no device memory.  d_bed, d_q, d_p,
 # d_ll and stream are device addresses / a CUstream handle.
