@@ -80,7 +80,8 @@ __global__ void k_sk_row(const uint8_t* __restrict__ bed, int64_t bps, int64_t c
 
 // Squared distances of every individual to KK centres (columns col0 .. col0+KK-1
 // of theta, row stride ldt) over the SNPs sel[0..nsel), summed in that order.
-// KK = 1: the distance goes to d_out; else the nearest centre to assign.
+// With d_out (KK = 1 only) the distance is written there; otherwise the
+// nearest centre goes to assign.
 template <int KK>
 __global__ void __launch_bounds__(SK_THREADS)
 k_sk_dist(const uint8_t* __restrict__ bed, int64_t bps, int64_t I, const double* __restrict__ T,
@@ -101,7 +102,7 @@ k_sk_dist(const uint8_t* __restrict__ bed, int64_t bps, int64_t I, const double*
             acc[j] = __dadd_rn(acc[j], __dmul_rn(d, d));
         }
     }
-    if (KK == 1) {
+    if (d_out) {
         d_out[i] = acc[0];
         return;
     }
@@ -154,6 +155,8 @@ __global__ void k_sk_mask(double* __restrict__ theta, const uint8_t* __restrict_
 
 cudaError_t launch_dist(int K, int64_t I, const uint8_t* bed, int64_t bps, const double* T, const double* theta,
                         int ldt, int col0, const int64_t* sel, int64_t nsel, int* assign, double* d_out) {
+    // exactly one output: a distance (one centre) or an assignment
+    if ((d_out != nullptr) == (assign != nullptr) || (d_out && K != 1)) return cudaErrorInvalidValue;
     const unsigned g = (unsigned)((I + SK_THREADS - 1) / SK_THREADS);
 #define HX_SK_CASE(KK)                                                                                         \
     case KK:                                                                                                   \

@@ -38,13 +38,18 @@ def test_skfr_matches_oracle(hx, O, case):
 
 
 def test_skfr_rejects_bad_sizes(hx):
+    """Refused on the host, before any device work."""
     from haplo_gb300 import _lib, skfr
     c = small_cohort(20, 6, 2, seed=55)
-    for K, s in ((21, 2), (2, 7), (2, 0)):
+    for K, s in ((2, 7), (2, 0)):             # sparsity outside 1..6 blocks
         with pytest.raises(hx.HxError) as e:
             skfr.select_aims(c["bed"], 20, K, s)
         assert e.value.status == _lib.HX_EINVAL
-    with pytest.raises(hx.HxError) as e:
+    tiny = small_cohort(5, 6, 2, seed=56)
+    with pytest.raises(hx.HxError) as e:      # more clusters than individuals
+        skfr.select_aims(tiny["bed"], 5, 6, 2)
+    assert e.value.status == _lib.HX_EINVAL
+    with pytest.raises(hx.HxError) as e:      # K beyond HX_KMAX
         skfr.select_aims(c["bed"], 20, 13, 2)
     assert e.value.status == _lib.HX_EUNSUPPORTED
 
