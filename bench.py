@@ -66,6 +66,9 @@ def parse(argv=None):
                          "to convergence (the default, about 11 minutes at I=1e5, J=1e5, K=8)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the planned grid splits (no hx_autotune)")
+    ap.add_argument("--skfr", type=int, default=0, metavar="SPARSITY",
+                    help="also time the AIM selection (hx_skfr) of SPARSITY blocks on the cohort, with the CPU "
+                         "oracle on the same input beside it (oracle memory grows as I x SNPs: small configs)")
     ap.add_argument("--cpu-full-fit", action="store_true",
                     help="also fit the whole cohort with the CPU oracle from the same start (measured, not "
                          "extrapolated; hours at I=1e5, J=1e5; minutes at I=1e4, J=5e4)")
@@ -544,6 +547,22 @@ def run_ours(args, world, rank, local):
                       "scaled by J/%d; I-only pieces (per-individual QPs, projections) and the ZAL point at full "
                       "size; summed with this fit's %d EM + %d outer iterations (extrapolated)"
                       % (threads, I, Js, Js, args.em_iters, iters)}
+    if args.skfr and rank == 0:
+        from haplo_gb300 import skfr
+        hb = bed_dev.cpu().numpy().reshape(n_snp, bps)
+        t0 = time.perf_counter()
+        cl, aims, sit = skfr.select_aims(hb, I, K, args.skfr, seed=0, device=local)
+        t_gpu = time.perf_counter() - t0
+        row = {"sparsity_blocks": args.skfr, "K": K, "iterations": sit, "gpu_s": t_gpu,
+               "note": "wall time of hx_skfr from host bytes (upload, k-means++ start, iterations)"}
+        if not args.no_cpu:
+            from oracle import skfr_oracle
+            t0 = time.perf_counter()
+            oc, oa, oit = skfr_oracle.select(hb, I, K, args.skfr, seed=0)
+            row.update({"cpu_s": time.perf_counter() - t0, "cpu_kind": "port (numpy oracle, one host thread "
+                        "for the per-SNP loops)", "identical_to_oracle": bool(np.array_equal(oa, aims) and
+                                                                             np.array_equal(oc, cl) and oit == sit)})
+        line["skfr"] = row
     if args.cpu_full_fit and rank == 0:
         from oracle import oracle as O
         threads = os.cpu_count() or 1
