@@ -37,10 +37,13 @@ def fit_many(ctxs, n_iter=1000, rtol=1e-7, em_iters=5, threads=0):
 
 
 def k_sweep(bed, I, J, Ks, restarts=4, seed=0, precision="mixed", n_iter=1000, rtol=1e-7, em_iters=5,
-            threads=0, keep=False, **create):
+            threads=0, keep=False, autotune=False, **create):
     """Fits every K in Ks from `restarts` random starts (random_init with seed
     seed + 1000 K + r).  Returns a list of dicts (K, restart, ll, aic, iters,
-    converged, and q, p when keep=True), in (K, restart) order."""
+    converged, and q, p when keep=True), in (K, restart) order.  With
+    autotune (mixed method), the first fit of each K tunes the grid splits of
+    that K's passes at its start (hx_autotune) before the other restarts of
+    the K are created, so they start with the same splits."""
     Ks = [int(k) for k in Ks]
     parent = GB300Admix(bed, I, J, Ks[0], precision=precision, **create)
     ctxs, specs = [], []
@@ -49,6 +52,9 @@ def k_sweep(bed, I, J, Ks, restarts=4, seed=0, precision="mixed", n_iter=1000, r
             d = parent if (K == Ks[0] and r == 0) else GB300Admix.shared(parent, K, precision=precision)
             q0, p0 = random_init(I, J, K, np.random.default_rng(seed + 1000 * K + r))
             d.set_qp(q0, p0)
+            if autotune and r == 0 and precision == "mixed":
+                d.autotune()
+                d.set_qp(q0, p0)
             ctxs.append(d)
             specs.append((K, r))
     infos = fit_many(ctxs, n_iter=n_iter, rtol=rtol, em_iters=em_iters, threads=threads)
@@ -81,6 +87,7 @@ def _main():
     ap.add_argument("--rtol", type=float, default=1e-7)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--sequential", action="store_true", help="also time the fits one after another")
+    ap.add_argument("--autotune", action="store_true", help="tune each K's grid splits on its first fit")
     a = ap.parse_args()
     lo, hi = (int(x) for x in a.Ks.split("-"))
     Ks = list(range(lo, hi + 1))
@@ -92,11 +99,13 @@ def _main():
     synth.synth_device(cfg["seed"], cfg["Q"], cfg["P"], cfg["miss"], dev.data_ptr())
     bed = dev.cpu().numpy().reshape(2 * J, bps)
     t0 = time.time()
-    rows = k_sweep(bed, I, J, Ks, restarts=a.restarts, precision=a.precision, rtol=a.rtol, threads=a.threads)
+    rows = k_sweep(bed, I, J, Ks, restarts=a.restarts, precision=a.precision, rtol=a.rtol, threads=a.threads,
+                   autotune=a.autotune)
     t_batch = time.time() - t0
     for r in rows:
         print(json.dumps(r))
     summary = {"config": a.config, "I": I, "J": J, "Ks": a.Ks, "restarts": a.restarts, "fits": len(rows),
+               "autotune": a.autotune, "outer_iters": sum(r["iters"] for r in rows),
                "seconds_concurrent": t_batch, "best_K_by_aic": min(rows, key=lambda r: r["aic"])["K"]}
     if a.sequential:
         t0 = time.time()
