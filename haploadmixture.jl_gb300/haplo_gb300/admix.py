@@ -341,7 +341,7 @@ class AdmixResult:
 
 def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, skfr_max_inner_iter=50, skfr_seed=0,
                   admix_n_iter=1000, admix_rtol=1e-7, admix_n_em_iters=5, precision="fp64", Q=3, init_q=None,
-                  init_p=None, device=0, verbose=False, return_handle=False):
+                  init_p=None, fix_q=False, fix_p=False, device=0, verbose=False, return_handle=False):
     """src/driver.jl:38-79 with the _admixture_base sequence (133-201) on the
     GPU: load the .bed (first I individuals, first 2J SNPs), random start,
     init_em! unless both init_q and init_p are given, then admixture_qn!
@@ -352,7 +352,10 @@ def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, sk
     ranking on blocks of 2 SNPs, `skfr_max_inner_iter` iterations, start from
     `skfr_seed`), the file is filtered to them as
     <prefix>_<K>_<2*sparsity>aims.bed, and the fit reads that file; clusters
-    and aims are returned.  Without it they are None."""
+    and aims are returned.  Without it they are None.
+
+    fix_q / fix_p hold that factor during admixture_qn! (not during
+    init_em!, as _admixture_base passes them, src/driver.jl:181-197)."""
     if not str(filename).endswith(".bed"):
         raise ValueError("filename should end with .bed")
     rng = np.random.default_rng(rng) if not isinstance(rng, np.random.Generator) else rng
@@ -375,6 +378,8 @@ def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, sk
         d.init_em(admix_n_em_iters)
     if init_q is not None or init_p is not None:
         d.set_qp(init_q, init_p)
+    if fix_q or fix_p:
+        d.set_loop_opts(fix_q=fix_q, fix_p=fix_p)
     info = d.admixture_qn(admix_n_iter, admix_rtol)
     info["seconds"] = time.time() - t0
     res = AdmixResult(d, info)

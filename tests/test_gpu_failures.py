@@ -115,3 +115,20 @@ def test_run_admixture_from_disk_matches_oracle(hx, O, tmp_path, precision):
     assert abs(res.info["iters"] - oit) <= 1
     assert np.abs(res.q - oq).max() < 1e-5
     assert np.abs(res.p - op).max() < 1e-5
+
+
+def test_run_admixture_fix_p_with_injected_start(hx, O, tmp_path):
+    """fix_p with init_q/init_p (no init_em!): P stays at init_p and the fit
+    equals the oracle's admixture_qn! with fix_p from the same start."""
+    from haplo_gb300 import bed as bedio
+    from haplo_gb300.admix import run_admixture, random_init
+    I, J, K = 120, 30, 3
+    c = small_cohort(I, J, K, seed=45)
+    path = bedio.write_bed(str(tmp_path / "c"), c["bed"], I)
+    q0, p0 = random_init(I, J, K, np.random.default_rng(9))
+    res, _, _ = run_admixture(path, I, J, K, init_q=q0, init_p=p0, fix_p=True, admix_rtol=1e-8)
+    assert np.abs(res.p - p0).max() < 1e-12      # held (the QN point's projection may touch the last bits)
+    oq, op, oll, oit, _ = O.fit(O.Bed(c["bed"], I, J), K, q0, p0, n_iter=1000, rtol=1e-8, em_iters=0, fix_p=True)
+    assert res.ll_new == pytest.approx(oll, rel=1e-9)
+    assert np.abs(res.q - oq).max() < 1e-6
+    assert np.abs(res.p - op).max() < 1e-12
