@@ -81,12 +81,12 @@ __global__ void k_sk_row(const uint8_t* __restrict__ bed, int64_t bps, int64_t c
 // Squared distances of every individual to KK centres (columns col0 .. col0+KK-1
 // of theta, row stride ldt) over the SNPs sel[0..nsel), summed in that order.
 // With d_out (KK = 1 only) the distance is written there; otherwise the
-// nearest centre goes to assign.
+// nearest centre goes to assign and, with dmin, its distance to dmin.
 template <int KK>
 __global__ void __launch_bounds__(SK_THREADS)
 k_sk_dist(const uint8_t* __restrict__ bed, int64_t bps, int64_t I, const double* __restrict__ T,
           const double* __restrict__ theta, int ldt, int col0, const int64_t* __restrict__ sel, int64_t nsel,
-          int* __restrict__ assign, double* __restrict__ d_out) {
+          int* __restrict__ assign, double* __restrict__ d_out, double* __restrict__ dmin) {
     const int64_t i = (int64_t)blockIdx.x * SK_THREADS + threadIdx.x;
     if (i >= I) return;
     double acc[KK];
@@ -111,6 +111,7 @@ k_sk_dist(const uint8_t* __restrict__ bed, int64_t bps, int64_t I, const double*
     for (int j = 1; j < KK; ++j)
         if (acc[j] < acc[best]) best = j;
     assign[i] = best;
+    if (dmin) dmin[i] = acc[best];
 }
 
 // Per SNP (one warp each): counts of codes 0, 2, 3 per cluster, then the
@@ -154,13 +155,14 @@ __global__ void k_sk_mask(double* __restrict__ theta, const uint8_t* __restrict_
 }
 
 cudaError_t launch_dist(int K, int64_t I, const uint8_t* bed, int64_t bps, const double* T, const double* theta,
-                        int ldt, int col0, const int64_t* sel, int64_t nsel, int* assign, double* d_out) {
+                        int ldt, int col0, const int64_t* sel, int64_t nsel, int* assign, double* d_out,
+                        double* dmin = nullptr) {
     // exactly one output: a distance (one centre) or an assignment
     if ((d_out != nullptr) == (assign != nullptr) || (d_out && K != 1)) return cudaErrorInvalidValue;
     const unsigned g = (unsigned)((I + SK_THREADS - 1) / SK_THREADS);
 #define HX_SK_CASE(KK)                                                                                         \
     case KK:                                                                                                   \
-        k_sk_dist<KK><<<g, SK_THREADS>>>(bed, bps, I, T, theta, ldt, col0, sel, nsel, assign, d_out);          \
+        k_sk_dist<KK><<<g, SK_THREADS>>>(bed, bps, I, T, theta, ldt, col0, sel, nsel, assign, d_out, dmin);    \
         break;
     switch (K) {
         HX_SK_CASE(1) HX_SK_CASE(2) HX_SK_CASE(3) HX_SK_CASE(4) HX_SK_CASE(5) HX_SK_CASE(6)
@@ -205,7 +207,7 @@ int sk_status(cudaError_t e) {
 
 extern "C" int hx_skfr(const uint8_t* bed, int64_t bytes_per_snp, int64_t n_snp, int64_t I, int32_t K,
                        int64_t sparsity, int32_t max_iter, uint64_t seed, int32_t device, int32_t* clusters,
-                       int64_t* aims, int32_t* iters) {
+                       int64_t* aims, int32_t* iters, double* objective) {
     using namespace hx;
     const int64_t M = n_snp - n_snp % 2, nb = M / 2;
     if (!bed || !clusters || !aims || I < 1 || bytes_per_snp < (I + 3) / 4 || n_snp < 2 || max_iter < 1)
@@ -289,13 +291,20 @@ extern "C" int hx_skfr(const uint8_t* bed, int64_t bytes_per_snp, int64_t n_snp,
         k_sk_mask<<<(unsigned)std::min<int64_t>((M * K + 255) / 256, 4096), 256>>>(theta, keep, M, K);
         HX_SK_CK(cudaGetLastError());
         HX_SK_CK(cudaMemcpy(sel, kept.data(), kept.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-        HX_SK_CK(launch_dist(K, I, d_bed, bytes_per_snp, T, theta, K, 0, sel, (int64_t)kept.size(), assign, nullptr));
+        HX_SK_CK(launch_dist(K, I, d_bed, bytes_per_snp, T, theta, K, 0, sel, (int64_t)kept.size(), assign, nullptr,
+                             d2));
         HX_SK_CK(cudaMemcpy(hn_assign.data(), assign, (size_t)I * sizeof(int), cudaMemcpyDeviceToHost));
         const bool changed = hn_assign != ha;
         ha.swap(hn_assign);
         if (!changed) break;
     }
     if (it > max_iter) it = max_iter;
+    if (objective) {   // within-cluster sum of squares over the kept SNPs, summed in individual order
+        HX_SK_CK(cudaMemcpy(hd.data(), d2, (size_t)I * sizeof(double), cudaMemcpyDeviceToHost));
+        double w = 0.0;
+        for (int64_t i = 0; i < I; ++i) w += hd[i];
+        *objective = w;
+    }
     std::copy(ha.begin(), ha.end(), clusters);
     std::copy(kept.begin(), kept.end(), aims);
     if (iters) *iters = it;

@@ -78,7 +78,7 @@ SIGNATURES = {
     "hx_em_p_accum": (I32, [P, P, P, P]),
     "hx_set_wait_budget": (I32, [P, I64]),
     "hx_autotune": (I32, [P, P]),
-    "hx_skfr": (I32, [P, I64, I64, I64, I32, I64, I32, C.c_uint64, I32, P, P, C.POINTER(I32)]),
+    "hx_skfr": (I32, [P, I64, I64, I64, I32, I64, I32, C.c_uint64, I32, P, P, C.POINTER(I32), D]),
     "hx_qp_q": (I32, [P, I64, P, P, P, P]),
     "hx_qp_p": (I32, [P, I64, P, P, P, P]),
     "hx_project_q": (I32, [P, I64, P]),

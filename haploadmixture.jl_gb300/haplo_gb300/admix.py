@@ -339,7 +339,8 @@ class AdmixResult:
         self.I, self.J, self.K = d.I, d.J, d.K
 
 
-def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, skfr_max_inner_iter=50, skfr_seed=0,
+def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, skfr_tries=1, skfr_max_inner_iter=50,
+                  skfr_seed=0,
                   admix_n_iter=1000, admix_rtol=1e-7, admix_n_em_iters=5, precision="fp64", Q=3, init_q=None,
                   init_p=None, fix_q=False, fix_p=False, device=0, verbose=False, return_handle=False):
     """src/driver.jl:38-79 with the _admixture_base sequence (133-201) on the
@@ -350,7 +351,7 @@ def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, sk
     With `sparsity` (the reference's SKFR branch, :60-73 and 84-105), the
     AIMs are selected first (haplo_gb300.skfr: sparse k-means with feature
     ranking on blocks of 2 SNPs, `skfr_max_inner_iter` iterations, start from
-    `skfr_seed`), the file is filtered to them as
+    `skfr_seed`, the best of `skfr_tries` starts), the file is filtered to them as
     <prefix>_<K>_<2*sparsity>aims.bed, and the fit reads that file; clusters
     and aims are returned.  Without it they are None.
 
@@ -364,7 +365,7 @@ def run_admixture(filename, I, J, K, *, rng=None, sparsity=None, prefix=None, sk
         from . import skfr
         data, n_ind, n_snp = bedio.read_bed(filename)
         clusters, aims, _ = skfr.select_aims(data, n_ind, K, sparsity, seed=skfr_seed,
-                                             max_iter=skfr_max_inner_iter, device=device)
+                                             max_iter=skfr_max_inner_iter, device=device, tries=skfr_tries)
         filename = skfr.write_filtered(prefix or str(filename)[:-4], data, n_ind, K, aims)
     data, n_ind, n_snp = bedio.read_bed(filename)
     if I > n_ind or 2 * J > n_snp:

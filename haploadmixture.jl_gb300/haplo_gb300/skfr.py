@@ -17,19 +17,35 @@ from . import _lib
 from . import bed as bedio
 
 
-def select_aims(bed, I, K, sparsity, seed=0, max_iter=50, device=0):
-    """(clusters (I,) int32, aims (2*sparsity,) int64 sorted, iterations) for
-    the first I individuals of a (n_snp, ceil(N/4)) uint8 BED matrix."""
+def select_once(bed, I, K, sparsity, seed=0, max_iter=50, device=0):
+    """One run of hx_skfr: (clusters (I,) int32, aims (2*sparsity,) int64
+    sorted, iterations, within-cluster sum of squares over the kept SNPs)."""
     b = np.ascontiguousarray(bed, dtype=np.uint8)
     if b.ndim != 2:
         raise ValueError("bed must be a (n_snp, bytes_per_snp) matrix")
     clusters = np.zeros(int(I), dtype=np.int32)
     aims = np.zeros(2 * int(sparsity), dtype=np.int64)
     it = C.c_int32()
+    obj = C.c_double()
     st = _lib.load().hx_skfr(_lib.ptr(b), b.shape[1], b.shape[0], int(I), int(K), int(sparsity), int(max_iter),
-                             int(seed) % (1 << 64), int(device), _lib.ptr(clusters), _lib.ptr(aims), C.byref(it))
+                             int(seed) % (1 << 64), int(device), _lib.ptr(clusters), _lib.ptr(aims), C.byref(it),
+                             C.byref(obj))
     _lib.check(st)
-    return clusters, aims, int(it.value)
+    return clusters, aims, int(it.value), float(obj.value)
+
+
+def select_aims(bed, I, K, sparsity, seed=0, max_iter=50, device=0, tries=1):
+    """(clusters (I,) int32, aims (2*sparsity,) int64 sorted, iterations) for
+    the first I individuals of a (n_snp, ceil(N/4)) uint8 BED matrix.  With
+    tries > 1 (the reference's skfr_tries, sparsekmeans_repeat), the runs
+    start from seeds seed + 1000 t and the one with the smallest within-
+    cluster sum of squares is kept (the first on ties)."""
+    best = None
+    for t in range(max(1, int(tries))):
+        r = select_once(bed, I, K, sparsity, seed=int(seed) + 1000 * t, max_iter=max_iter, device=device)
+        if best is None or r[3] < best[3]:
+            best = r
+    return best[0], best[1], best[2]
 
 
 def filter_bed(bed, snps):

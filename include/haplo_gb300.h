@@ -244,10 +244,13 @@ int hx_fit_many(hx_ctx* const* ctxs, int32_t n, int32_t n_iter, double rtol, int
  * SNPs; an odd last SNP is ignored).  Genotypes are standardised per SNP
  * (missing -> mean), the start is k-means++ with uniform draws
  * SplitMix64(seed + t), and `sparsity` blocks are kept.  Outputs: clusters
- * (I entries, 0..K-1), aims (2 * sparsity sorted SNP indices), *iters
- * (optional).  HX_EINVAL for K > I or sparsity outside 1..n_snp/2. */
+ * (I entries, 0..K-1), aims (2 * sparsity sorted SNP indices), *iters and
+ * *objective (optional: the within-cluster sum of squares over the kept SNPs,
+ * which sparsekmeans_repeat compares across tries).  HX_EINVAL for K > I or
+ * sparsity outside 1..n_snp/2. */
 int hx_skfr(const uint8_t* bed, int64_t bytes_per_snp, int64_t n_snp, int64_t I, int32_t K, int64_t sparsity,
-            int32_t max_iter, uint64_t seed, int32_t device, int32_t* clusters, int64_t* aims, int32_t* iters);
+            int32_t max_iter, uint64_t seed, int32_t device, int32_t* clusters, int64_t* aims, int32_t* iters,
+            double* objective);
 
 /* Tile-shape autotuner of the mixed method (no reference counterpart): times
  * the Q and P tensor-core passes and the FP32 log-likelihood pass at the

@@ -298,9 +298,11 @@ function gb300_skfr(data::AbstractMatrix{UInt8}, I::Integer, K::Integer, sparsit
     clusters = zeros(Int32, I)
     aims = zeros(Int64, 2 * sparsity)
     iters = Ref{Int32}(0)
+    wcss = Ref{Float64}(0.0)
     st = ccall((:hx_skfr, libhx), Cint,
-               (Ptr{UInt8}, Int64, Int64, Int64, Int32, Int64, Int32, UInt64, Int32, Ptr{Int32}, Ptr{Int64}, Ref{Int32}),
-               data, size(data, 1), size(data, 2), I, K, sparsity, max_iter, seed, device, clusters, aims, iters)
+               (Ptr{UInt8}, Int64, Int64, Int64, Int32, Int64, Int32, UInt64, Int32, Ptr{Int32}, Ptr{Int64}, Ref{Int32},
+                Ref{Float64}),
+               data, size(data, 1), size(data, 2), I, K, sparsity, max_iter, seed, device, clusters, aims, iters, wcss)
     st == 0 || error("haplo_gb300: hx_skfr: ", unsafe_string(ccall((:hx_status_string, libhx), Cstring, (Cint,), st)))
     clusters .+ 1, aims .+ 1
 end

@@ -86,8 +86,10 @@ def _dist(x_rows, theta, snps):
     return d
 
 
-def select(bed, I, K, sparsity, seed=0, max_iter=50):
-    """(clusters (I,), aims (2*sparsity,) sorted SNP indices, iterations)."""
+def select(bed, I, K, sparsity, seed=0, max_iter=50, return_objective=False):
+    """(clusters (I,), aims (2*sparsity,) sorted SNP indices, iterations), and
+    with return_objective the within-cluster sum of squares over the kept
+    SNPs (each individual's distance to its centre, summed in order)."""
     M = bed.shape[0] - bed.shape[0] % 2
     nb = M // 2
     if not (1 <= K <= I) or not (1 <= sparsity <= nb):
@@ -134,9 +136,13 @@ def select(bed, I, K, sparsity, seed=0, max_iter=50):
         mask = np.zeros(M, dtype=bool)
         mask[keep] = True
         theta[~mask] = 0.0
-        new = np.argmin(_dist(X, theta, keep), axis=1)
+        dk = _dist(X, theta, keep)
+        new = np.argmin(dk, axis=1)
         changed = bool(np.any(new != assign))
         assign = new
         if not changed:
             break
-    return assign.astype(np.int32), keep.astype(np.int64), it
+    out = (assign.astype(np.int32), keep.astype(np.int64), it)
+    if return_objective:
+        out = out + (float(np.cumsum(dk[np.arange(I), assign])[-1]),)
+    return out

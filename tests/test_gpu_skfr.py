@@ -30,11 +30,17 @@ def test_skfr_matches_oracle(hx, O, case):
         c = small_cohort(240, 40, 5, seed=54, miss=0.02)
         I, K, s, bed = 240, 12, 12, c["bed"]
     for seed in (0, 7):
-        gc, ga, gi = skfr.select_aims(bed, I, K, s, seed=seed, max_iter=30)
-        oc, oa, oi = S.select(bed, I, K, s, seed=seed, max_iter=30)
+        gc, ga, gi, gw = skfr.select_once(bed, I, K, s, seed=seed, max_iter=30)
+        oc, oa, oi, ow = S.select(bed, I, K, s, seed=seed, max_iter=30, return_objective=True)
         np.testing.assert_array_equal(ga, oa)
         np.testing.assert_array_equal(gc, oc)
-        assert gi == oi
+        assert gi == oi and gw == ow
+    # several tries keep the start with the smallest within-cluster sum of squares
+    runs = [S.select(bed, I, K, s, seed=1000 * t, max_iter=30, return_objective=True) for t in range(3)]
+    best = min(range(3), key=lambda t: (runs[t][3], t))
+    tc, ta, _ = skfr.select_aims(bed, I, K, s, seed=0, max_iter=30, tries=3)
+    np.testing.assert_array_equal(ta, runs[best][1])
+    np.testing.assert_array_equal(tc, runs[best][0])
 
 
 def test_skfr_rejects_bad_sizes(hx):
